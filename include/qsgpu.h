@@ -1,0 +1,155 @@
+/*
+ * qsgpu.h -- C ABI of libqsgpu.so, the GB300 (sm_103a) hot path of QuSpin's
+ * symmetry-reduced Hamiltonian apply, expm_multiply_parallel and Lanczos.
+ *
+ * All pointers named d_* or documented as "device" are CUDA device pointers
+ * owned by the caller; `stream` is a cudaStream_t (NULL = legacy stream).
+ * Every function returns 0 on success or a negative status:
+ *   -1 invalid argument, -2 CUDA error, -3 unknown operator character,
+ *   -4 complex element in a real dtype, -5 buffer too small,
+ *   -6 unsupported configuration, -7 iteration cap reached.
+ * Element type codes: 0 float32, 1 float64, 2 complex64, 3 complex128.
+ *
+ * Each declaration names the reference interface it replaces (QuSpin 1.0.1;
+ * paths relative to the reference project root; "html" = the Sphinx
+ * viewcode copy of the un-vendored parallel-sparse-tools 0.2.5 wrappers,
+ * docs/modules/parallel_sparse_tools/...).
+ */
+#ifndef QSGPU_H
+#define QSGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- symmetry context ------------------------------------------------
+ * Replaces the construction of the native basis core
+ * (hcb_basis_core_wrap / spinless_fermion_basis_core_wrap at
+ * src/quspin/basis/basis_general/base_hcb.py:74-76 and fermion.py:178-180):
+ * per-bit site maps (negative = inversion), periods, quantum numbers and the
+ * phase tables exp(-2 pi i p / L), cos(2 pi p / L), L = lcm(periods). */
+int qs_sym_create(int N, int fermion, int nmaps, const int32_t *maps, const int32_t *pers, const int32_t *qs,
+                  const double *phase_re, const double *phase_im, const double *costab, int L, void **out);
+int qs_sym_destroy(void *sym);
+
+/* ---- prefix sums (device int64, in place) ------------------------------ */
+int64_t qs_scan_scratch_elems(int64_t n);
+int qs_scan_inclusive_i64(int64_t *x, int64_t n, int64_t *scratch, void *stream);
+
+/* ---- basis enumeration: _core.make_basis (base_general.py:862-867) ------
+ * kind 0: all 2^N words; 1: popcount == p0; 2: spinful, p0 ones in the high
+ * N/2 bits and p1 in the low N/2 bits.  States come out sorted descending,
+ * as the reference keeps them (base_general.py:875-885). */
+int64_t qs_enum_num_candidates(int N, int kind, int p0, int p1);
+int64_t qs_enum_num_chunks(int N, int kind, int p0, int p1);
+int qs_enum_count(void *sym, int kind, int p0, int p1, int64_t *d_off, int64_t nchunks, int64_t *d_scratch,
+                  int64_t *h_total, void *stream);
+int qs_enum_write(void *sym, int kind, int p0, int p1, const int64_t *d_off, int64_t nchunks, void *d_states,
+                  uint32_t *d_norms, void *stream);
+
+/* ---- _core.make_basis_blocks (base_general.py:944-947) ------------------ */
+int qs_make_blocks(int N, int state_bytes, int N_p, const void *d_states, int64_t Ns, int64_t *d_begin,
+                   int64_t *d_end, void *stream);
+
+/* ---- _get_basis_index (base_general.py:281-285) ------------------------- */
+int qs_index(int N, int state_bytes, const void *d_states, int64_t Ns, int N_p, const int64_t *d_begin,
+             const int64_t *d_end, const void *d_queries, int64_t nq, int64_t *d_out, void *stream);
+
+/* ---- _core.representative (base_general.py:1085-1117) ------------------- */
+int qs_representative(void *sym, const void *d_states, int64_t n, void *d_out, int32_t *d_g_out, int8_t *d_sign_out,
+                      void *stream);
+
+/* ---- _core.normalization (base_general.py:1158-1181) -------------------- */
+int qs_normalization(void *sym, const void *d_states, int64_t n, uint32_t *d_out, void *stream);
+
+/* ---- _core.op (base_general.py:324-336): one operator-string term -------
+ * Term table (device): nop[t], off[t] into chr/site, J[2t..2t+1]. */
+int qs_op(void *sym, const void *d_states, const uint32_t *d_norms, int64_t Ns, int N_p, const int64_t *d_begin,
+          const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off, const int8_t *t_chr,
+          const int32_t *t_site, const double *t_J, int64_t *d_row, int64_t *d_col, double *d_ME, int *d_err,
+          void *stream);
+
+/* ---- canonical CSR assembly: basis._make_matrix (src/quspin/basis/base.py:265-304)
+ * count -> inclusive scan -> fill -> merge -> inclusive scan -> compact. */
+int qs_csr_count(void *sym, int vtype, const void *d_states, const uint32_t *d_norms, int64_t Ns, int N_p,
+                 const int64_t *d_begin, const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off,
+                 const int8_t *t_chr, const int32_t *t_site, const double *t_J, int T, int64_t *d_rowcnt,
+                 int *d_term_flags, int *d_err, void *stream);
+int qs_csr_fill(void *sym, int vtype, const void *d_states, const uint32_t *d_norms, int64_t Ns, int N_p,
+                const int64_t *d_begin, const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off,
+                const int8_t *t_chr, const int32_t *t_site, const double *t_J, int T, const int64_t *d_rowptr,
+                int64_t *d_cursor, uint64_t *d_keys, void *d_vals, int *d_err, void *stream);
+int qs_csr_diag(void *sym, int vtype, const void *d_states, const uint32_t *d_norms, int64_t Ns, int N_p,
+                const int64_t *d_begin, const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off,
+                const int8_t *t_chr, const int32_t *t_site, const double *t_J, int T, void *d_diag,
+                int *d_term_flags, int *d_err, void *stream);
+int qs_csr_merge(int vtype, int64_t Ns, const int64_t *d_rowptr, uint64_t *d_keys, void *d_vals,
+                 const void *d_diag, int64_t *d_mcount, int *d_err, void *stream);
+int qs_csr_compact(int vtype, int64_t Ns, const int64_t *d_rowptr, const uint64_t *d_keys, const void *d_vals,
+                   const int64_t *d_incl, void *d_indptr, int idx64, int32_t *d_indices, void *d_data,
+                   void *stream);
+
+/* ---- _core.inplace_op (base_general.py:395-408): matrix-free apply ------ */
+int qs_inplace_op(void *sym, const void *d_states, const uint32_t *d_norms, int64_t Ns, int N_p,
+                  const int64_t *d_begin, const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off,
+                  const int8_t *t_chr, const int32_t *t_site, const double *t_J, int T, int transposed,
+                  int conjugated, double a_re, double a_im, const void *d_vin, void *d_vout, int64_t nvec,
+                  int *d_err, void *stream);
+
+/* ---- _matvec for csr / dia (html matvec/matvec_core.html:146-201) ------- */
+int qs_csr_matvec(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                  const void *d_data, int dtype, const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re,
+                  double a_im, int overwrite, int group, void *stream);
+int qs_dia_matvec(int64_t n, int ndiag, const int64_t *d_offsets, int64_t ldd, const void *d_data, int dtype,
+                  const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re, double a_im, int overwrite,
+                  void *stream);
+
+/* ---- reductions: numpy vdot / norm of the Lanczos recurrence
+ * (src/quspin/tools/lanczos/_lanczos_utils.py:180-204) ------------------ */
+int qs_reduce_scratch_doubles(void);
+int qs_vdot(int64_t n, const void *d_x, const void *d_y, int cplx, double *d_out, double *d_scratch, void *stream);
+int qs_nrm2(int64_t n2, const void *d_x, double *d_out, double *d_scratch, void *stream);
+
+/* ---- _wrapper_csr_trace / _wrapper_csr_1_norm
+ * (html expm_multiply_parallel_core.html:196-202) ---------------------- */
+int qs_csr_trace(int64_t n, const void *d_indptr, int idx64, const int32_t *d_indices, const void *d_data, int cplx,
+                 double *d_out, double *d_scratch, void *stream);
+int qs_csr_1_norm(int64_t n, const void *d_indptr, int idx64, const int32_t *d_indices, const void *d_data, int cplx,
+                  double sh_re, double sh_im, double *d_out, double *d_colsum, double *d_scratch, void *stream);
+
+/* ---- _wrapper_expm_multiply / _wrapper_expm_multiply_batch
+ * (html expm_multiply_parallel_core.html:347-372) ----------------------- */
+int qs_expm_ctl_bytes(void);
+int qs_taylor_term(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                   const void *d_data, int dtype, const void *d_Bin, void *d_Bout, int btype, void *d_F,
+                   int64_t nvec, double mu_re, double mu_im, const void *d_coeff, int j, double tol, void *d_ctl,
+                   int group, void *stream);
+int qs_taylor_rescale(int64_t n, int64_t nvec, void *d_F, void *d_B0, int btype, const void *d_eta, void *d_ctl,
+                      void *stream);
+int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                     const void *d_data, int dtype, void *d_F, int64_t nvec, int s, int m_star, double tol,
+                     double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
+                     void *d_work, int btype, void *d_ctl, int group, void *stream);
+
+/* ---- Lanczos recurrence steps: lanczos_full / lanczos_iter
+ * (src/quspin/tools/lanczos/_lanczos_utils.py:158-204, :283-311), the
+ * optional full reorthogonalisation, and lin_comb_Q_T (:366-425).  Vectors
+ * are float64 or complex128 (cplx); n2 counts doubles (2n if complex). --- */
+int qs_lanczos_ctl_bytes(void);
+int qs_lanczos_scratch_doubles(void);
+int64_t qs_lanczos_reorth_scratch_doubles(int nk);
+int qs_lanczos_scale(int64_t n2, const double *d_r, const double *d_b, double *d_q, const void *d_ctl, void *stream);
+int qs_lanczos_alpha(int64_t n, int cplx, double *d_r, const double *d_v, const double *d_b, const double *d_q,
+                     double *d_a_out, double *d_scratch, void *d_ctl, void *stream);
+int qs_lanczos_beta(int64_t n2, double *d_r, const double *d_a, const double *d_q, int do_axpy, double *d_b_out,
+                    double eps, int i, double *d_scratch, void *d_ctl, void *stream);
+int qs_lanczos_reorth(int64_t n, int cplx, int nk, const double *d_Q, int64_t ldq, double *d_r, int passes,
+                      double *d_scratch, void *d_ctl, void *stream);
+int qs_lanczos_lincomb(int64_t n_el, int nk, const double *d_c, int cplx_c, const double *d_Q, int64_t ldq,
+                       int cplx_q, double *d_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSGPU_H */

@@ -1,0 +1,120 @@
+"""Device plumbing: torch tensors as CUDA buffers, streams, dtype codes."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_NP_TO_CODE = {
+    np.dtype(np.float32): _lib.F32,
+    np.dtype(np.float64): _lib.F64,
+    np.dtype(np.complex64): _lib.C64,
+    np.dtype(np.complex128): _lib.C128,
+}
+_NP_TO_TORCH = {
+    np.dtype(np.float32): torch.float32,
+    np.dtype(np.float64): torch.float64,
+    np.dtype(np.complex64): torch.complex64,
+    np.dtype(np.complex128): torch.complex128,
+    np.dtype(np.int32): torch.int32,
+    np.dtype(np.int64): torch.int64,
+    np.dtype(np.int8): torch.int8,
+    np.dtype(np.uint8): torch.uint8,
+    np.dtype(np.uint32): torch.int32,     # reinterpreted bit patterns
+    np.dtype(np.uint64): torch.int64,
+}
+_TORCH_TO_NP = {
+    torch.float32: np.dtype(np.float32),
+    torch.float64: np.dtype(np.float64),
+    torch.complex64: np.dtype(np.complex64),
+    torch.complex128: np.dtype(np.complex128),
+    torch.int32: np.dtype(np.int32),
+    torch.int64: np.dtype(np.int64),
+    torch.int8: np.dtype(np.int8),
+    torch.uint8: np.dtype(np.uint8),
+}
+
+SUPPORTED = (np.dtype(np.float32), np.dtype(np.float64), np.dtype(np.complex64), np.dtype(np.complex128))
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("quspin_gb300 needs a CUDA device (sm_103a); none is available")
+    _lib.load()
+
+
+def device():
+    require_cuda()
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def code(dtype):
+    return _NP_TO_CODE[np.dtype(dtype)]
+
+
+def torch_dtype(dtype):
+    return _NP_TO_TORCH[np.dtype(dtype)]
+
+
+def np_dtype(tdtype):
+    return _TORCH_TO_NP[tdtype]
+
+
+def stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ptr(t):
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def empty(shape, dtype):
+    return torch.empty(shape, dtype=torch_dtype(dtype), device=device())
+
+
+def zeros(shape, dtype):
+    return torch.zeros(shape, dtype=torch_dtype(dtype), device=device())
+
+
+def to_device(a, dtype=None):
+    """Contiguous device tensor from a numpy array / torch tensor / scalar list."""
+    if isinstance(a, torch.Tensor):
+        t = a
+        if dtype is not None and t.dtype != torch_dtype(dtype):
+            t = t.to(torch_dtype(dtype))
+        if not t.is_cuda:
+            t = t.to(device(), non_blocking=False)
+        return t.contiguous()
+    arr = np.asarray(a)
+    if dtype is not None:
+        arr = arr.astype(dtype, copy=False)
+    if arr.dtype == np.uint32:
+        arr = arr.view(np.int32)
+    elif arr.dtype == np.uint64:
+        arr = arr.view(np.int64)
+    return torch.from_numpy(np.ascontiguousarray(arr)).to(device())
+
+
+def to_host(t, dtype=None):
+    arr = t.detach().cpu().numpy()
+    if dtype is not None and arr.dtype != np.dtype(dtype):
+        arr = arr.view(dtype) if arr.dtype.itemsize == np.dtype(dtype).itemsize and \
+            arr.dtype.kind in "iu" and np.dtype(dtype).kind in "iu" else arr.astype(dtype)
+    return arr
+
+
+def is_device_array(x):
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def scratch_doubles(n):
+    return torch.empty(max(int(n), 1), dtype=torch.float64, device=device())
+
+
+def err_flag():
+    return torch.zeros(1, dtype=torch.int32, device=device())

@@ -1,0 +1,358 @@
+// Truncated-Taylor action of the matrix exponential, e^{aA} v, on the GPU.
+//
+// Replaces the native loop QuSpin 1.0.1 runs through
+// parallel-sparse-tools==0.2.5 (_wrapper_expm_multiply and
+// _wrapper_expm_multiply_batch, called at
+// docs/modules/parallel_sparse_tools/expm_multiply_parallel_core/
+// expm_multiply_parallel_core.html:347-372).  Its contract, which the
+// reference's tests pin against scipy at 1e-15 (test/test_expm_multiply_parallel.py:65-74),
+// is scipy's _expm_multiply_simple_core with the shift folded into the
+// product (html :392-396):
+//
+//   F = v; B = v; eta = exp(a mu / s)
+//   repeat s times:
+//     c1 = ||B||_inf
+//     for j < m*:  B = a/(s(j+1)) (A B - mu B);  c2 = ||B||_inf;  F += B
+//                  stop if c1 + c2 <= tol ||F||_inf;  c1 = c2
+//     F = eta F;  B = F
+//
+// One launch per Taylor term does the whole term: CSR apply, shift, scale,
+// accumulate into F and both infinity norms (row sums of moduli over the k
+// right-hand sides).  The last block of each launch evaluates the stopping
+// test in a small device control block, so the host never synchronises;
+// launches after the test has fired return immediately.  B may be stored in
+// complex64 (the mixed form) while F, mu, the coefficients and the norms stay
+// in double precision.
+#include "qs_common.cuh"
+
+struct ExpmCtl {
+    double c1;                 // ||B||_inf at the start of the current term
+    unsigned long long c2;     // running max row-norm of the new term (bits of a double >= 0)
+    unsigned long long fn;     // running max row-norm of F
+    int done;                  // stopping test fired in this substep
+    unsigned int arrive;       // blocks finished in the current launch
+    long long terms;           // Taylor terms executed so far
+};
+
+extern "C" int qs_expm_ctl_bytes() { return (int)sizeof(ExpmCtl); }
+
+template <typename T> struct BLoad;
+template <> struct BLoad<cdbl> {
+    __device__ static cdbl ld(const cdbl *p, int64_t i) {
+        double2 v = __ldg(reinterpret_cast<const double2 *>(p) + i);
+        return cdbl{v.x, v.y};
+    }
+    __device__ static void st(cdbl *p, int64_t i, cdbl v) { p[i] = v; }
+};
+template <> struct BLoad<cflt> {
+    __device__ static cdbl ld(const cflt *p, int64_t i) {
+        float2 v = __ldg(reinterpret_cast<const float2 *>(p) + i);
+        return cdbl{(double)v.x, (double)v.y};
+    }
+    __device__ static void st(cflt *p, int64_t i, cdbl v) { p[i] = cflt{(float)v.x, (float)v.y}; }
+};
+template <typename T> struct DLoad;
+template <> struct DLoad<double> { __device__ static double ld(const double *p, int64_t i) { return __ldg(p + i); } };
+template <> struct DLoad<float> { __device__ static double ld(const float *p, int64_t i) { return (double)__ldg(p + i); } };
+template <> struct DLoad<cdbl> {
+    __device__ static cdbl ld(const cdbl *p, int64_t i) {
+        double2 v = __ldg(reinterpret_cast<const double2 *>(p) + i);
+        return cdbl{v.x, v.y};
+    }
+};
+template <> struct DLoad<cflt> {
+    __device__ static cdbl ld(const cflt *p, int64_t i) {
+        float2 v = __ldg(reinterpret_cast<const float2 *>(p) + i);
+        return cdbl{(double)v.x, (double)v.y};
+    }
+};
+
+__device__ __forceinline__ void madd(cdbl &acc, double d, cdbl x) { acc.x += d * x.x; acc.y += d * x.y; }
+__device__ __forceinline__ void madd(cdbl &acc, cdbl d, cdbl x)
+{
+    acc.x += d.x * x.x - d.y * x.y;
+    acc.y += d.x * x.y + d.y * x.x;
+}
+
+__device__ __forceinline__ double cabs_(cdbl v) { return sqrt(v.x * v.x + v.y * v.y); }
+
+// block-wide max of two non-negative doubles, atomically folded into ctl
+__device__ __forceinline__ void fold_max2(double a, double b, unsigned long long *ga, unsigned long long *gb)
+{
+    __shared__ double sa[32], sb[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
+        b = fmax(b, __shfl_down_sync(0xffffffffu, b, o));
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sa[w] = a; sb[w] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ma = 0.0, mb = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { ma = fmax(ma, sa[k]); mb = fmax(mb, sb[k]); }
+        if (ga) atomicMax(ga, (unsigned long long)__double_as_longlong(ma));
+        if (gb) atomicMax(gb, (unsigned long long)__double_as_longlong(mb));
+    }
+}
+
+// returns true in thread 0 of the last block to arrive
+__device__ __forceinline__ bool last_block(ExpmCtl *ctl)
+{
+    __shared__ bool is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int t = atomicAdd(&ctl->arrive, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return is_last;
+}
+
+template <typename DT, typename BT, typename IT, int G, int NB>
+__global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *__restrict__ indptr,
+                                                          const int32_t *__restrict__ indices,
+                                                          const DT *__restrict__ data, const BT *__restrict__ Bin,
+                                                          BT *__restrict__ Bout, cdbl *__restrict__ F, int64_t nvec,
+                                                          cdbl mu, const cdbl *__restrict__ coeff, int j,
+                                                          double tol, ExpmCtl *ctl)
+{
+    if (*((volatile int *)&ctl->done)) return;
+    const cdbl cf = coeff[j];
+    const int lane = threadIdx.x & (G - 1);
+    const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+    double mb = 0.0, mf = 0.0;
+    for (int64_t r = group; r < n; r += ngroups) {
+        const int64_t k0 = indptr[r], k1 = indptr[r + 1];
+        double rb = 0.0, rf = 0.0;
+        for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
+            cdbl acc[NB];
+#pragma unroll
+            for (int b = 0; b < NB; b++) acc[b] = cdbl{0.0, 0.0};
+            for (int64_t k = k0 + lane; k < k1; k += G) {
+                const int64_t col = __ldg(indices + k);
+                const auto d = DLoad<DT>::ld(data, k);
+#pragma unroll
+                for (int b = 0; b < NB; b++)
+                    if (c0 + b < nvec) madd(acc[b], d, BLoad<BT>::ld(Bin, col * nvec + c0 + b));
+            }
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    acc[b].x += __shfl_down_sync(0xffffffffu, acc[b].x, o, G);
+                    acc[b].y += __shfl_down_sync(0xffffffffu, acc[b].y, o, G);
+                }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    if (c0 + b >= nvec) break;
+                    const int64_t e = r * nvec + c0 + b;
+                    const cdbl bo = BLoad<BT>::ld(Bin, e);
+                    // w = A B - mu B
+                    const double wr = acc[b].x - (mu.x * bo.x - mu.y * bo.y);
+                    const double wi = acc[b].y - (mu.x * bo.y + mu.y * bo.x);
+                    cdbl bn{cf.x * wr - cf.y * wi, cf.x * wi + cf.y * wr};
+                    BLoad<BT>::st(Bout, e, bn);
+                    cdbl f = F[e];
+                    f.x += bn.x; f.y += bn.y;
+                    F[e] = f;
+                    rb += cabs_(bn);
+                    rf += cabs_(f);
+                }
+            }
+        }
+        mb = fmax(mb, rb);
+        mf = fmax(mf, rf);
+    }
+    fold_max2(mb, mf, &ctl->c2, &ctl->fn);
+    if (last_block(ctl) && threadIdx.x == 0) {
+        volatile ExpmCtl *vc = ctl;
+        double c2 = __longlong_as_double((long long)vc->c2);
+        double fn = __longlong_as_double((long long)vc->fn);
+        vc->terms = vc->terms + 1;
+        if (vc->c1 + c2 <= tol * fn) vc->done = 1;
+        else vc->c1 = c2;
+        vc->c2 = 0ull;
+        vc->fn = 0ull;
+        __threadfence();
+        vc->arrive = 0u;
+    }
+}
+
+// F = eta F; B0 = F; ctl->c1 = ||F||_inf; ctl->done = 0.
+template <typename BT>
+__global__ void __launch_bounds__(256) taylor_rescale_kernel(int64_t n, int64_t nvec, cdbl *__restrict__ F,
+                                                             BT *__restrict__ B0, const cdbl *__restrict__ eta_p,
+                                                             ExpmCtl *ctl)
+{
+    const cdbl eta = *eta_p;
+    const bool scale = !(eta.x == 1.0 && eta.y == 0.0);
+    double m = 0.0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double rs = 0.0;
+        for (int64_t c = 0; c < nvec; c++) {
+            const int64_t e = r * nvec + c;
+            cdbl f = F[e];
+            if (scale) {
+                cdbl g{eta.x * f.x - eta.y * f.y, eta.x * f.y + eta.y * f.x};
+                f = g;
+                F[e] = f;
+            }
+            BLoad<BT>::st(B0, e, f);
+            rs += cabs_(f);
+        }
+        m = fmax(m, rs);
+    }
+    fold_max2(m, 0.0, &ctl->c2, nullptr);
+    if (last_block(ctl) && threadIdx.x == 0) {
+        volatile ExpmCtl *vc = ctl;
+        vc->c1 = __longlong_as_double((long long)vc->c2);
+        vc->c2 = 0ull;
+        vc->fn = 0ull;
+        vc->done = 0;
+        __threadfence();
+        vc->arrive = 0u;
+    }
+}
+
+static int pick_group_e(int64_t n, int64_t nnz)
+{
+    double avg = n > 0 ? (double)nnz / (double)n : 1.0;
+    if (avg >= 24) return 32;
+    if (avg >= 12) return 16;
+    if (avg >= 6) return 8;
+    return 4;
+}
+
+static int grid_for(int64_t n, int G)
+{
+    int64_t gpb = 256 / G;
+    int64_t b = (n + gpb - 1) / gpb;
+    int64_t cap = (int64_t)qs_num_sms() * 8;   // 8 resident blocks of 256 threads per SM
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+template <typename DT, typename BT, typename IT, int NB>
+static int term_launch(int64_t n, int64_t nnz, const void *indptr, const int32_t *indices, const void *data,
+                       const void *Bin, void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j,
+                       double tol, ExpmCtl *ctl, int G, cudaStream_t st)
+{
+    int blocks = grid_for(n, G);
+#define L_(GG) taylor_term_kernel<DT, BT, IT, GG, NB><<<blocks, 256, 0, st>>>(n, (const IT *)indptr, indices, (const DT *)data, (const BT *)Bin, (BT *)Bout, F, nvec, mu, coeff, j, tol, ctl)
+    switch (G) {
+    case 4: L_(4); break;
+    case 8: L_(8); break;
+    case 16: L_(16); break;
+    default: L_(32); break;
+    }
+#undef L_
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+template <typename DT, typename BT, typename IT>
+static int term_nb(int64_t n, int64_t nnz, const void *indptr, const int32_t *indices, const void *data,
+                   const void *Bin, void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j, double tol,
+                   ExpmCtl *ctl, int G, cudaStream_t st)
+{
+    if (nvec == 1) return term_launch<DT, BT, IT, 1>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    if (nvec == 2) return term_launch<DT, BT, IT, 2>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    if (nvec <= 4) return term_launch<DT, BT, IT, 4>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    return term_launch<DT, BT, IT, 8>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+}
+
+template <typename DT, typename BT>
+static int term_idx(int idx64, int64_t n, int64_t nnz, const void *indptr, const int32_t *indices, const void *data,
+                    const void *Bin, void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j, double tol,
+                    ExpmCtl *ctl, int G, cudaStream_t st)
+{
+    if (idx64) return term_nb<DT, BT, int64_t>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    return term_nb<DT, BT, int32_t>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+}
+
+// One Taylor term (see file header).  dtype: value type of A (QS_F64,
+// QS_C128, QS_F32, QS_C64); btype: storage of B (QS_C128 or QS_C64); F is
+// complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
+// ctl: device control block (qs_expm_ctl_bytes()).
+extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
+                              const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
+                              int64_t nvec, double mu_re, double mu_im, const void *coeff, int j, double tol,
+                              void *ctl, int group, void *stream)
+{
+    if (n < 1 || nvec < 1 || !indptr || !Bin || !Bout || !F || !coeff || !ctl || j < 0) return QS_ERR_ARG;
+    int G = group > 0 ? group : pick_group_e(n, nnz);
+    if (G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
+    cdbl mu{mu_re, mu_im};
+    cudaStream_t st = qs_stream(stream);
+    ExpmCtl *c = reinterpret_cast<ExpmCtl *>(ctl);
+    const cdbl *cf = reinterpret_cast<const cdbl *>(coeff);
+    cdbl *Fp = reinterpret_cast<cdbl *>(F);
+    if (btype == QS_C128) {
+        switch (dtype) {
+        case QS_F64: return term_idx<double, cdbl>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        case QS_C128: return term_idx<cdbl, cdbl>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        default: return QS_ERR_ARG;
+        }
+    } else if (btype == QS_C64) {
+        switch (dtype) {
+        case QS_F32: return term_idx<float, cflt>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        case QS_C64: return term_idx<cflt, cflt>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        case QS_F64: return term_idx<double, cflt>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        default: return QS_ERR_ARG;
+        }
+    }
+    return QS_ERR_ARG;
+}
+
+// F = eta F; B0 = F; c1 = ||F||_inf; done = 0 (eta: device complex128).
+// With eta = 1 this is the set-up before the first substep.
+extern "C" int qs_taylor_rescale(int64_t n, int64_t nvec, void *F, void *B0, int btype, const void *eta, void *ctl,
+                                 void *stream)
+{
+    if (n < 1 || nvec < 1 || !F || !B0 || !eta || !ctl) return QS_ERR_ARG;
+    cudaStream_t st = qs_stream(stream);
+    int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
+    int blocks = (int)(b > cap ? cap : b);
+    if (btype == QS_C128)
+        taylor_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, (const cdbl *)eta,
+                                                           (ExpmCtl *)ctl);
+    else if (btype == QS_C64)
+        taylor_rescale_kernel<cflt><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cflt *)B0, (const cdbl *)eta,
+                                                           (ExpmCtl *)ctl);
+    else return QS_ERR_ARG;
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+// Full e^{aA} v in place on F (complex128 [n, nvec]): s substeps of at most
+// m_star terms.  work: two B buffers of n*nvec elements of btype; coeff:
+// device complex128[max(m_star,1)] with coeff[j] = a / (s (j+1)); eta: device
+// complex128 = exp(a mu / s); one: device complex128 = 1.  ctl zeroed by the
+// caller before the first call.  No host synchronisation.
+extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
+                                const void *data, int dtype, void *F, int64_t nvec, int s, int m_star, double tol,
+                                double mu_re, double mu_im, const void *coeff, const void *eta, const void *one,
+                                void *work, int btype, void *ctl, int group, void *stream)
+{
+    if (n < 1 || nvec < 1 || s < 1 || m_star < 0 || !work || !ctl) return QS_ERR_ARG;
+    size_t esz = btype == QS_C128 ? 16 : 8;
+    char *b0 = reinterpret_cast<char *>(work);
+    char *b1 = b0 + (size_t)n * nvec * esz;
+    int rc = qs_taylor_rescale(n, nvec, F, b0, btype, one, ctl, stream);
+    if (rc) return rc;
+    for (int i = 0; i < s; i++) {
+        for (int j = 0; j < m_star; j++) {
+            void *bin = (j & 1) ? b1 : b0;
+            void *bout = (j & 1) ? b0 : b1;
+            rc = qs_taylor_term(n, nnz, indptr, idx64, indices, data, dtype, bin, bout, btype, F, nvec, mu_re, mu_im,
+                                coeff, j, tol, ctl, group, stream);
+            if (rc) return rc;
+        }
+        rc = qs_taylor_rescale(n, nvec, F, b0, btype, eta, ctl, stream);
+        if (rc) return rc;
+    }
+    return QS_OK;
+}

@@ -1,0 +1,47 @@
+// Common definitions for the GB300 hot-path library (libqsgpu.so).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define QS_OK 0
+#define QS_ERR_ARG -1        // invalid argument (sizes, pointers, enums)
+#define QS_ERR_CUDA -2       // a CUDA runtime call failed
+#define QS_ERR_OPSTR -3      // unknown operator character
+#define QS_ERR_COMPLEX -4    // complex matrix element requested in a real dtype
+#define QS_ERR_CAPACITY -5   // output buffer too small
+#define QS_ERR_UNSUPPORTED -6
+#define QS_ERR_NOT_CONVERGED -7
+
+// value / vector element types shared with the Python side
+#define QS_F32 0
+#define QS_F64 1
+#define QS_C64 2
+#define QS_C128 3
+
+#define QS_CHECK(call)                                   \
+    do {                                                 \
+        cudaError_t e__ = (call);                        \
+        if (e__ != cudaSuccess) return QS_ERR_CUDA;      \
+    } while (0)
+
+static inline cudaStream_t qs_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+static inline int qs_num_sms()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    return sms;
+}
+
+// complex helpers (plain structs; no std::complex in device code)
+struct cdbl { double x, y; };
+struct cflt { float x, y; };
+
+template <typename T> struct is_cplx { static constexpr bool value = false; };
+template <> struct is_cplx<cdbl> { static constexpr bool value = true; };
+template <> struct is_cplx<cflt> { static constexpr bool value = true; };

@@ -1,0 +1,188 @@
+"""Device-resident sparse matrices (CSR and DIA) and their products.
+
+``DeviceCSR`` holds the canonical CSR that the GPU Hamiltonian builder
+produces (int32 or int64 ``indptr``, int32 ``indices``, values in one of
+float32/float64/complex64/complex128) and applies it with the kernels of
+``csrc/sparse.cu`` -- the GPU counterpart of parallel-sparse-tools' ``_matvec``
+(docs/modules/parallel_sparse_tools/matvec/matvec_core.html:146-201 in the
+reference).  ``DeviceDIA`` is the diagonal storage the reference uses when every
+term of an operator is diagonal (src/quspin/basis/base.py:299-304).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _device as D
+from . import _lib
+
+
+def result_dtype(*dtypes):
+    return np.result_type(*[np.dtype(d) for d in dtypes])
+
+
+class DeviceCSR:
+    format = "csr"
+
+    def __init__(self, indptr, indices, data, shape, dtype):
+        self.indptr = indptr
+        self.indices = indices
+        self.data = data
+        self.shape = (int(shape[0]), int(shape[1]))
+        self.dtype = np.dtype(dtype)
+        self.idx64 = 1 if indptr.dtype == torch.int64 else 0
+        self._nnz = None
+
+    @property
+    def nnz(self):
+        if self._nnz is None:
+            self._nnz = int(self.indptr[-1].item()) if self.shape[0] > 0 else 0
+        return self._nnz
+
+    @classmethod
+    def from_scipy(cls, A, dtype=None):
+        A = sp.csr_matrix(A)
+        if dtype is not None:
+            A = A.astype(dtype)
+        if not A.has_canonical_format:
+            A = A.copy()
+            A.sum_duplicates()
+        dt = np.dtype(A.dtype)
+        if dt not in D.SUPPORTED:
+            dt = result_dtype(dt, np.float64)
+            A = A.astype(dt)
+        ip = A.indptr.astype(np.int32 if A.nnz < 2**31 - 1 else np.int64)
+        return cls(D.to_device(ip), D.to_device(A.indices.astype(np.int32)), D.to_device(A.data),
+                   A.shape, dt)
+
+    def tocsr(self):
+        """Host scipy.sparse.csr_matrix copy."""
+        return sp.csr_matrix((D.to_host(self.data), D.to_host(self.indices), D.to_host(self.indptr)),
+                             shape=self.shape)
+
+    def astype(self, dtype):
+        dtype = np.dtype(dtype)
+        if dtype == self.dtype:
+            return self
+        return DeviceCSR(self.indptr, self.indices, self.data.to(D.torch_dtype(dtype)), self.shape, dtype)
+
+    def matvec_into(self, x, y, a=1.0, overwrite=True, group=0):
+        """y (=|+=) a * A x on device tensors of the result dtype."""
+        n = self.shape[0]
+        nvec = 1 if x.dim() == 1 else x.shape[1]
+        xt = D.np_dtype(x.dtype)
+        a = complex(a)
+        _lib.call("qs_csr_matvec", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
+                  D.ptr(self.data), D.code(self.dtype), D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,
+                  int(bool(overwrite)), int(group), D.stream())
+        return y
+
+    def dot(self, V, out=None, a=1.0, overwrite_out=True):
+        return _apply(self, V, out, a, overwrite_out)
+
+    def trace(self):
+        if self.dtype not in (np.dtype(np.float64), np.dtype(np.complex128)):
+            return self.astype(result_dtype(self.dtype, np.float64)).trace()
+        out = D.zeros(2, np.float64)
+        scr = D.scratch_doubles(_lib.load().qs_reduce_scratch_doubles())
+        _lib.call("qs_csr_trace", self.shape[0], D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
+                  D.ptr(self.data), int(self.dtype.kind == "c"), D.ptr(out), D.ptr(scr), D.stream())
+        o = out.cpu().numpy()
+        return complex(o[0], o[1]) if self.dtype.kind == "c" else float(o[0])
+
+    def onenorm(self, shift=0.0):
+        """max_c sum_r |A + shift I|[r, c]."""
+        if self.dtype not in (np.dtype(np.float64), np.dtype(np.complex128)):
+            return self.astype(result_dtype(self.dtype, np.float64)).onenorm(shift)
+        shift = complex(shift)
+        out = D.zeros(1, np.float64)
+        col = D.scratch_doubles(self.shape[0])
+        scr = D.scratch_doubles(_lib.load().qs_reduce_scratch_doubles())
+        _lib.call("qs_csr_1_norm", self.shape[0], D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
+                  D.ptr(self.data), int(self.dtype.kind == "c"), shift.real, shift.imag, D.ptr(out), D.ptr(col),
+                  D.ptr(scr), D.stream())
+        return float(out.item())
+
+
+class DeviceDIA:
+    format = "dia"
+
+    def __init__(self, offsets, data, shape, dtype):
+        self.offsets = offsets      # int64 [ndiag] device
+        self.data = data            # [ndiag, ldd] device
+        self.shape = (int(shape[0]), int(shape[1]))
+        self.dtype = np.dtype(dtype)
+
+    @classmethod
+    def from_diagonal(cls, diag, dtype):
+        n = diag.shape[0]
+        return cls(D.to_device(np.zeros(1, np.int64)), diag.reshape(1, n).contiguous(), (n, n), dtype)
+
+    @classmethod
+    def from_scipy(cls, A, dtype=None):
+        A = sp.dia_matrix(A)
+        if dtype is not None:
+            A = A.astype(dtype)
+        return cls(D.to_device(A.offsets.astype(np.int64)), D.to_device(np.ascontiguousarray(A.data)),
+                   A.shape, A.dtype)
+
+    @property
+    def nnz(self):
+        return int(self.data.numel())
+
+    def tocsr(self):
+        return sp.dia_matrix((D.to_host(self.data), D.to_host(self.offsets)), shape=self.shape).tocsr()
+
+    def astype(self, dtype):
+        dtype = np.dtype(dtype)
+        if dtype == self.dtype:
+            return self
+        return DeviceDIA(self.offsets, self.data.to(D.torch_dtype(dtype)), self.shape, dtype)
+
+    def matvec_into(self, x, y, a=1.0, overwrite=True, group=0):
+        n = self.shape[0]
+        nvec = 1 if x.dim() == 1 else x.shape[1]
+        a = complex(a)
+        _lib.call("qs_dia_matvec", n, int(self.offsets.numel()), D.ptr(self.offsets), int(self.data.shape[1]),
+                  D.ptr(self.data), D.code(self.dtype), D.ptr(x), D.code(D.np_dtype(x.dtype)), D.ptr(y), nvec,
+                  a.real, a.imag, int(bool(overwrite)), D.stream())
+        return y
+
+    def dot(self, V, out=None, a=1.0, overwrite_out=True):
+        return _apply(self, V, out, a, overwrite_out)
+
+    def trace(self):
+        return self.tocsr().diagonal().sum()
+
+
+def to_device_matrix(A, dtype=None):
+    if isinstance(A, (DeviceCSR, DeviceDIA)):
+        return A if dtype is None else A.astype(dtype)
+    if sp.issparse(A) and A.format == "dia":
+        return DeviceDIA.from_scipy(A, dtype)
+    return DeviceCSR.from_scipy(A, dtype)
+
+
+def _apply(M, V, out, a, overwrite_out):
+    """matvec with numpy-or-device operands; numpy in -> numpy out."""
+    host = not D.is_device_array(V)
+    rdt = result_dtype(M.dtype, V.dtype if host else D.np_dtype(V.dtype))
+    if rdt not in D.SUPPORTED:
+        rdt = result_dtype(rdt, np.float64)
+    if np.iscomplexobj(np.zeros(1, rdt)) is False and np.iscomplexobj(a):
+        rdt = result_dtype(rdt, np.complex64)
+    x = D.to_device(V, rdt)
+    if out is None:
+        y = torch.empty_like(x)
+        overwrite_out = True
+    else:
+        y = out if D.is_device_array(out) else D.to_device(out, rdt)
+    M.matvec_into(x, y, a=a, overwrite=overwrite_out)
+    if host:
+        res = D.to_host(y)
+        if out is not None and not D.is_device_array(out):
+            out[...] = res
+            return out
+        return res
+    return y
