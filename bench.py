@@ -1,0 +1,427 @@
+"""Benchmark: expm_multiply evolutions/s on the L=32 J1-J2 Heisenberg chain.
+
+Workload (one "step" = one evolution): J1-J2 chain, L=32, J1=1, J2=0.5,
+periodic, sector Sz=0, k=0, p=+1, z=+1 (4,707,969 states, <= 65 nonzeros per
+row, float64 CSR with int32 indices); e^{-iHt} applied to a seeded,
+normalised complex128 Gaussian state with t=5.0 through
+ExpmMultiplyParallel.dot -- the call QuSpin users make
+(quspin.tools.expm_multiply_parallel).
+
+  value      evolutions/s with the state resident in HBM (device timing,
+             CUDA events on the launching stream, synchronised on both sides)
+  e2e        the same through the public API with a host numpy state:
+             host->device copy of the state and device->host copy of the
+             result inside the timed region
+  roofline   the fused Taylor-term kernel (the dominant kernel): algorithmic
+             bytes per launch / average launch time, against the measured HBM
+             copy bandwidth
+  cpu_baseline  the oracle's OpenMP Taylor loop on the host cores, timed on a
+             bounded sample of Taylor terms of the same evolution
+
+The CSR (about 2.5 GB) is far larger than L2 (129 MB), so every Taylor term
+streams it from HBM; no separate L2 flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="j1j2_chain_L32_Sz0_k0_p+1_z+1_expm_t5", L=32, J1=1.0, J2=0.5, t=5.0,
+                sector="Sz=0,k=0,p=+1,z=+1", state="seeded normalised complex128 Gaussian (seed 0)",
+                l2="inputs larger than L2 (CSR ~2.5 GB streamed per Taylor term)")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def j1j2_static(L, J1, J2):
+    st = []
+    for op in ("+-", "-+"):
+        st.append([op, [[J1 / 2, i, (i + 1) % L] for i in range(L)] + [[J2 / 2, i, (i + 2) % L] for i in range(L)]])
+    st.append(["zz", [[J1, i, (i + 1) % L] for i in range(L)] + [[J2, i, (i + 2) % L] for i in range(L)]])
+    return st
+
+
+def chain_blocks(L):
+    s = np.arange(L)
+    return dict(kblock=((s + 1) % L, 0), pblock=(s[::-1].copy(), 0), zblock=(-(s + 1), 0))
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            for k in ("hbm_gbs", "hbm_GBs", "hbm_copy_gbs"):
+                if k in d:
+                    v = d[k]
+                    if isinstance(v, dict):
+                        v = v.get("burst", v.get("value"))
+                    return float(v), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per launch of the Taylor-term kernel from the committed ncu
+    summary (a 'traffic_bytes_per_launch_full: <int>' line), else None."""
+    p = os.path.join(ROOT, "profiles", "taylor_term_j1j2_L32.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch_full:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out = self.proc.communicate(timeout=5)[0]
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_setup(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws, device=None):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_problem(L, J1, J2):
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    b = spin_basis_general(L, Nup=L // 2, pauli=0, **chain_blocks(L))
+    H = hamiltonian(j1j2_static(L, J1, J2), [], basis=b, dtype=np.float64)
+    return b, H
+
+
+def taylor_term_bytes(n, nnz, nvec=1):
+    """Algorithmic bytes of one fused Taylor term, float64 values, int32
+    indices, complex128 B and F: values+indices once, indptr once, B gathered
+    once (compulsory), new B written, F read and written."""
+    return nnz * (8 + 4) + 4 * (n + 1) + n * nvec * (16 + 16 + 2 * 16)
+
+
+def spmv_bytes(n, nnz, nvec=1):
+    return nnz * (8 + 4) + 4 * (n + 1) + n * nvec * (16 + 16)
+
+
+def time_kernels(op, F, reps=20):
+    """Average device time of the Taylor-term kernel launched alone (stopping
+    test disabled) and of the plain SpMV, CUDA events on the launching stream."""
+    import torch
+    from quspin_gb300 import _device as D
+    from quspin_gb300 import _lib
+    A = op.A_device
+    n = A.shape[0]
+    st = torch.cuda.current_stream()
+    work = torch.empty(2 * n, dtype=torch.complex128, device=F.device)
+    b0, b1 = work[:n], work[n:]
+    b0.copy_(F)
+    Fw = F.clone()
+    ctl = torch.zeros(6, dtype=torch.int64, device=F.device)
+    ctl.view(torch.float64)[0] = float("inf")          # c1 = inf: the stopping test never fires
+    coeff = torch.tensor([complex(op.a) / 1000.0], dtype=torch.complex128, device=F.device)
+    mu = complex(op._mu)
+
+    def launch(j):
+        bi, bo = (b0, b1) if j % 2 == 0 else (b1, b0)
+        _lib.call("qs_taylor_term", n, A.nnz, D.ptr(A.indptr), A.idx64, D.ptr(A.indices), D.ptr(A.data),
+                  D.code(A.dtype), D.ptr(bi), D.ptr(bo), _lib.C128, D.ptr(Fw), 1, mu.real, mu.imag, D.ptr(coeff),
+                  0, 0.0, D.ptr(ctl), 0, D.stream())
+    for j in range(3):
+        launch(j)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for j in range(reps):
+        launch(j)
+    e1.record(st)
+    torch.cuda.synchronize()
+    t_term = e0.elapsed_time(e1) / 1e3 / reps
+    y = torch.empty_like(F)
+    for _ in range(3):
+        A.matvec_into(F, y)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        A.matvec_into(F, y)
+    e1.record(st)
+    torch.cuda.synchronize()
+    t_spmv = e0.elapsed_time(e1) / 1e3 / reps
+    return t_term, t_spmv
+
+
+def cpu_baseline(H, op, terms_per_evolution, budget_s=12.0):
+    """Oracle OpenMP Taylor loop on the host cores over a bounded sample of
+    Taylor terms of this evolution; evolutions/s scaled by the executed term
+    count of the GPU run."""
+    from oracle import oracle as O
+    A = H.static.tocsr() if hasattr(H, "static") else H
+    ip, ix, dt, cp, n = O._csr_parts(A)
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=n) + 1j * rng.normal(size=n)
+    v /= np.linalg.norm(v)
+    L = O.lib()
+    a = complex(op.a)
+    mu = complex(op._mu)
+
+    def run(terms):
+        x = v.astype(np.complex128).copy()
+        w = np.zeros(2 * n, np.complex128)
+        t0 = time.perf_counter()
+        # s = 1, m* = terms, tol = 0: exactly `terms` Taylor terms
+        L.orc_expm_multiply(ip, ix, dt, cp, n, 1, 1, int(terms), 0.0, mu.real, mu.imag, a.real / 1000.0,
+                            a.imag / 1000.0, 1.0, 0.0, x.view(np.float64).reshape(-1),
+                            w.view(np.float64).reshape(-1))
+        return time.perf_counter() - t0
+    t2 = run(2)
+    k = int(max(2, min(200, budget_s / max(t2 / 2, 1e-6))))
+    tk = run(k)
+    per_term = tk / k
+    return {"value": 1.0 / (per_term * terms_per_evolution), "unit": "evolutions/s", "cores": int(O.num_threads()),
+            "kind": "port",
+            "sample": "{} fused Taylor terms of this evolution on the host (oracle OpenMP loop, {:.2f} s), scaled "
+                      "by the {} terms one GPU evolution executes".format(k, tk, terms_per_evolution),
+            "seconds_per_term": per_term}
+
+
+def run_ours(args, rank, ws):
+    import torch
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    W = WORKLOAD
+    t0 = time.perf_counter()
+    b, H = build_problem(W["L"], W["J1"], W["J2"])
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    A = H.tocsr_gpu()
+    n, nnz = A.shape[0], A.nnz
+    t0 = time.perf_counter()
+    np.random.seed(0)
+    op = ExpmMultiplyParallel(A, a=-1j * W["t"])
+    t_setup = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=n) + 1j * rng.normal(size=n)
+    v /= np.linalg.norm(v)
+    v_dev = torch.tensor(v, dtype=torch.complex128, device=dev)
+    F = torch.empty_like(v_dev)
+    for _ in range(args.warmup):
+        F.copy_(v_dev)
+        op.run_device(F)
+    torch.cuda.synchronize()
+    terms = op.terms_executed
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(args.steps):
+            F.copy_(v_dev)
+            op.run_device(F)
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier(ws)
+    T = e0.elapsed_time(e1) / 1e3
+    T = max_over_ranks(T, ws, dev)
+    # end to end through the public API with host buffers
+    for _ in range(1):
+        op.dot(v)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0.record(st)
+    for _ in range(args.steps):
+        w_host = op.dot(v)
+    e1.record(st)
+    torch.cuda.synchronize()
+    T_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
+    norm_err = abs(np.linalg.norm(w_host) - 1.0)
+    t_term, t_spmv = time_kernels(op, v_dev)
+    peak, peak_kind = peak_hbm()
+    tb = taylor_term_bytes(n, nnz)
+    achieved = tb / t_term / 1e9
+    launches_per_evolution = 2 + op.s * (op.m_star + 1)   # rescale + s (m* terms + rescale); copy excluded
+    out = {
+        "metric": "expm_multiply evolutions/s", "value": ws * args.steps / T, "unit": "evolutions/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian state; Hamiltonian exactly as configured)",
+        "config": dict(W, Ns=n, nnz=nnz, m_star=op.m_star, s=op.s, terms_per_evolution=terms,
+                       parallelism="replicas" if ws > 1 else "single", build_s=round(t_build, 3),
+                       expm_setup_s=round(t_setup, 3)),
+        "e2e": {"value": ws * args.steps / T_e2e, "unit": "evolutions/s", "h2d_bytes_per_step": int(n * 16),
+                "d2h_bytes_per_step": int(n * 16)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_term_kernel",
+                     "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
+                     "spmv_gbs": spmv_bytes(n, nnz) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv},
+        "gpu_launches": int(args.steps * launches_per_evolution),
+        "clocks": clk.summary(),
+        "state_norm_error": norm_err,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline(H, op, terms)
+        except Exception as e:  # report, never fake
+            out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_reference(args, rank, ws):
+    """The reference's CPU path (the oracle port of QuSpin's OpenMP basis,
+    CSR assembly and Taylor loop) on the host cores; each step a bounded
+    sample of Taylor terms of the same evolution."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    W = WORKLOAD
+    L = W["L"]
+    t0 = time.perf_counter()
+    ob = O.OracleBasis(L, [(1, L // 2, 0)], pauli=0, **chain_blocks(L))
+    A = ob.build_csr(O.consolidate_static(j1j2_static(L, W["J1"], W["J2"])), np.float64)
+    t_build = time.perf_counter() - t0
+    n = A.shape[0]
+    np.random.seed(0)
+    op = O.ExpmMultiplyParallelOracle(A, a=-1j * W["t"])
+    ip, ix, dt, cp, _ = O._csr_parts(A)
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=n) + 1j * rng.normal(size=n)
+    v /= np.linalg.norm(v)
+    Lb = O.lib()
+    a, mu = complex(op._a), complex(op._mu)
+    sample = 8
+
+    def step():
+        x = v.copy()
+        w = np.zeros(2 * n, np.complex128)
+        Lb.orc_expm_multiply(ip, ix, dt, cp, n, 1, 1, sample, 0.0, mu.real, mu.imag, a.real / 1000, a.imag / 1000,
+                             1.0, 0.0, x.view(np.float64).reshape(-1), w.view(np.float64).reshape(-1))
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    T = time.perf_counter() - t0
+    per_term = T / (args.steps * sample)
+    terms_bound = op._m_star * op._s
+    value = 1.0 / (per_term * terms_bound)
+    out = {"metric": "expm_multiply evolutions/s", "value": value, "unit": "evolutions/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded Gaussian state; Hamiltonian exactly as configured)", "impl": "reference",
+           "config": dict(W, Ns=n, nnz=int(A.nnz), m_star=int(op._m_star), s=int(op._s), build_s=round(t_build, 2)),
+           "cpu_baseline": {"value": value, "unit": "evolutions/s", "cores": int(O.num_threads()), "kind": "port",
+                            "sample": "each step = {} fused Taylor terms of the evolution (oracle OpenMP loop); "
+                                      "evolutions/s = 1 / (time per term x m* s = {} terms, the no-early-stop "
+                                      "count)".format(sample, terms_bound)},
+           "e2e": {"value": value, "unit": "evolutions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
+    args = p.parse_args()
+    if args.L != 32:
+        WORKLOAD["L"] = args.L
+        WORKLOAD["workload"] = "j1j2_chain_L{}_Sz0_k0_p+1_z+1_expm_t5".format(args.L)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        rank, ws = dist_setup("gloo")
+        run_reference(args, rank, ws)
+    else:
+        rank, ws = dist_setup("nccl")
+        run_ours(args, rank, ws)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

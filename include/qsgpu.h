@@ -84,8 +84,8 @@ int qs_csr_diag(void *sym, int vtype, const void *d_states, const uint32_t *d_no
                 const int64_t *d_begin, const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off,
                 const int8_t *t_chr, const int32_t *t_site, const double *t_J, int T, void *d_diag,
                 int *d_term_flags, int *d_err, void *stream);
-int qs_csr_merge(int vtype, int64_t Ns, const int64_t *d_rowptr, uint64_t *d_keys, void *d_vals,
-                 const void *d_diag, int64_t *d_mcount, int *d_err, void *stream);
+int qs_csr_merge(int vtype, int64_t Ns, const int64_t *d_rowptr, const int64_t *d_fillcnt, uint64_t *d_keys,
+                 void *d_vals, const void *d_diag, int64_t *d_mcount, int *d_err, void *stream);
 int qs_csr_compact(int vtype, int64_t Ns, const int64_t *d_rowptr, const uint64_t *d_keys, const void *d_vals,
                    const int64_t *d_incl, void *d_indptr, int idx64, int32_t *d_indices, void *d_data,
                    void *stream);

@@ -96,6 +96,13 @@ def lib():
                                             c.c_double, c.c_double, c.c_double, c.c_double,
                                             c.c_double, c.c_double, _f64p, _f64p]
             L.orc_expm_multiply.restype = c.c_int64
+            L.orc_build_csr.argtypes = sym + [_f64p, _f64p, c.c_int, _i32p, _i32p, c.c_char_p, _i32p, _f64p, _i32p,
+                                              _u64p, _u32p, c.c_int64, c.c_int, _i64p, _i64p, c.c_int,
+                                              c.POINTER(c.c_void_p), c.POINTER(c.c_void_p),
+                                              c.POINTER(c.c_void_p)]
+            L.orc_build_csr.restype = c.c_int64
+            L.orc_free.argtypes = [c.c_void_p]
+            L.orc_free.restype = None
             L.orc_num_threads.argtypes = []
             L.orc_num_threads.restype = c.c_int
             _lib = L
@@ -329,6 +336,36 @@ class OracleBasis:
             return sp.dia_matrix((np.atleast_2d(diag), [0]), shape=(Ns, Ns), dtype=dtype)
         return sp.dia_matrix((Ns, Ns), dtype=dtype)
 
+    def build_csr(self, op_list, dtype):
+        """make_matrix without scipy's pairwise additions (same arithmetic;
+        C + OpenMP), for large sectors.  float64 / complex128 only."""
+        dtype = np.dtype(dtype)
+        terms = [self._prep(o, ix, J) for o, ix, J in op_list]
+        T = len(terms)
+        nop = np.asarray([len(o) for o, _, _ in terms], np.int32)
+        off = np.concatenate([[0], np.cumsum(nop)[:-1]]).astype(np.int32)
+        chrs = "".join(o for o, _, _ in terms).encode()
+        site = np.concatenate([ix for _, ix, _ in terms]).astype(np.int32) if T else np.zeros(1, np.int32)
+        J = np.asarray([[complex(j).real, complex(j).imag] for _, _, j in terms], np.float64).reshape(-1)
+        is_diag = np.asarray([int(set(o) <= set("Izn")) for o, _, _ in terms], np.int32)
+        ip, ix_, dt = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        real = int(dtype.kind != "c")
+        nnz = lib().orc_build_csr(*self._symargs(), self.phase_re, self.phase_im, T, nop, off, chrs, site, J,
+                                  is_diag, self.states, self.norms, self.Ns, self.N_p, self.begin, self.end, real,
+                                  ctypes.byref(ip), ctypes.byref(ix_), ctypes.byref(dt))
+        if nnz < 0:
+            raise ValueError("bad operator string or symmetry map")
+        Ns = self.Ns
+        indptr = np.ctypeslib.as_array(ctypes.cast(ip, ctypes.POINTER(ctypes.c_int64)), (Ns + 1,)).copy()
+        indices = np.ctypeslib.as_array(ctypes.cast(ix_, ctypes.POINTER(ctypes.c_int32)), (max(nnz, 1),))[:nnz].copy()
+        vals = np.ctypeslib.as_array(ctypes.cast(dt, ctypes.POINTER(ctypes.c_double)),
+                                     ((1 if real else 2) * max(nnz, 1),)).copy()
+        for p_ in (ip, ix_, dt):
+            lib().orc_free(p_)
+        data = vals[:nnz] if real else vals[:2 * nnz].view(np.complex128)
+        itype = np.int32 if nnz < 2**31 - 1 else np.int64
+        return sp.csr_matrix((data.astype(dtype), indices, indptr.astype(itype)), shape=(Ns, Ns))
+
     def inplace_op(self, v_in, op_list, dtype, transposed=False, conjugated=False, a=1.0):
         v = np.asarray(v_in)
         squeeze = v.ndim == 1
@@ -430,7 +467,10 @@ class ExpmMultiplyParallelOracle:
         else:
             self._dtype = dtype
         self._tol = np.finfo(self._dtype).eps / 2
-        self._mu = np.array(csr_trace(self._A) / self._A.shape[0], dtype=self._dtype)
+        tr = csr_trace(self._A)
+        if np.dtype(self._dtype).kind != "c":
+            tr = tr.real
+        self._mu = np.array(tr / self._A.shape[0], dtype=self._dtype)
         self._A_1_norm = csr_1_norm(self._A, -complex(self._mu))
         self._calculate_partition()
 

@@ -54,7 +54,7 @@ _SIGS = {
     "qs_csr_fill": (_i, [_vp, _i, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp,
                          _vp, _vp]),
     "qs_csr_diag": (_i, [_vp, _i, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
-    "qs_csr_merge": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qs_csr_merge": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qs_csr_compact": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
     "qs_inplace_op": (_i, [_vp, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _vp,
                            _vp, _i64, _vp, _vp]),

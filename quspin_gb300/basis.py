@@ -547,6 +547,8 @@ def build_matrix(basis, op_list, dtype):
             return DeviceDIA(D.to_device(np.zeros(0, np.int64)), diag.reshape(0, Ns), (Ns, Ns), dtype)
         return DeviceDIA.from_diagonal(diag, dtype)
     tt = _TermTable([terms[i] for i in off_idx])
+    if diag is not None:
+        rowcnt[1:] += 1          # a spare slot per row for a diagonal entry the merge may add
     scr = torch.empty(max(L.qs_scan_scratch_elems(Ns), 1), dtype=torch.int64, device=D.device())
     _lib.call("qs_scan_inclusive_i64", D.ptr(rowcnt[1:]), Ns, D.ptr(scr), st)
     nnz_pre = int(rowcnt[-1].item())
@@ -555,12 +557,12 @@ def build_matrix(basis, op_list, dtype):
     cursor = torch.zeros(Ns, dtype=torch.int64, device=D.device())
     _lib.check(L.qs_csr_fill(basis._sym, vt, *basis._basis_args(), *tt.args(), tt.T, D.ptr(rowcnt), D.ptr(cursor),
                              D.ptr(keys), D.ptr(vals), D.ptr(err), st), "qs_csr_fill")
-    del cursor
     mcount = torch.empty(Ns, dtype=torch.int64, device=D.device())
-    _lib.check(L.qs_csr_merge(vt, Ns, D.ptr(rowcnt), D.ptr(keys), D.ptr(vals), D.ptr(diag), D.ptr(mcount),
-                              D.ptr(err), st), "qs_csr_merge")
+    _lib.check(L.qs_csr_merge(vt, Ns, D.ptr(rowcnt), D.ptr(cursor), D.ptr(keys), D.ptr(vals), D.ptr(diag),
+                              D.ptr(mcount), D.ptr(err), st), "qs_csr_merge")
     if int(err.item()) & 8:
         raise NotImplementedError("a matrix row collects more than 512 entries before merging")
+    del cursor
     _lib.call("qs_scan_inclusive_i64", D.ptr(mcount), Ns, D.ptr(scr), st)
     nnz = int(mcount[-1].item())
     idx64 = nnz >= 2**31 - 1

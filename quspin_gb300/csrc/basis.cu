@@ -1016,9 +1016,11 @@ __global__ void csr_diag_kernel(SymView<S> V, size_t tab_elems, BasisView B, Ter
 
 // One warp per row: bitonic sort of the row's keys in shared memory, then a
 // serial term-ordered merge by lane 0.  Merged (col, value) pairs overwrite
-// the row's range; mcount[r] receives their number.
+// the row's range; mcount[r] receives their number.  When a diagonal array is
+// given, each row range must hold one slot more than its scattered entries.
 template <typename T>
 __global__ void __launch_bounds__(128) csr_merge_kernel(int64_t Ns, const int64_t *__restrict__ rowptr,
+                                                        const int64_t *__restrict__ fillcnt,
                                                         uint64_t *__restrict__ keys, T *__restrict__ vals,
                                                         const T *__restrict__ diag, int64_t *__restrict__ mcount,
                                                         int *__restrict__ d_err)
@@ -1029,8 +1031,10 @@ __global__ void __launch_bounds__(128) csr_merge_kernel(int64_t Ns, const int64_
     const int64_t nwarps = (int64_t)gridDim.x * 4;
     for (int64_t r = (int64_t)blockIdx.x * 4 + wib; r < Ns; r += nwarps) {
         const int64_t p0 = rowptr[r], p1 = rowptr[r + 1];
-        const int len = (int)(p1 - p0);
-        if (len > ROW_SORT_MAX) {
+        // fillcnt[r] entries were scattered into [p0, p1); with a diagonal
+        // array the row range holds one spare slot for a new diagonal entry
+        const int len = (int)(fillcnt ? fillcnt[r] : (p1 - p0));
+        if (len > ROW_SORT_MAX || (diag && (int64_t)len + 1 > p1 - p0)) {
             if (lane == 0) atomicOr(d_err, 8);
             continue;
         }
@@ -1250,26 +1254,30 @@ extern "C" int qs_csr_diag(void *sym, int vtype, const void *states, const uint3
 }
 
 template <typename T>
-static int csr_merge_t(int64_t Ns, const int64_t *rowptr, uint64_t *keys, void *vals, const void *diag,
-                       int64_t *mcount, int *d_err, cudaStream_t st)
+static int csr_merge_t(int64_t Ns, const int64_t *rowptr, const int64_t *fillcnt, uint64_t *keys, void *vals,
+                       const void *diag, int64_t *mcount, int *d_err, cudaStream_t st)
 {
     int64_t blocks = (Ns + 3) / 4;
     int64_t cap = (int64_t)qs_num_sms() * 16;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    csr_merge_kernel<T><<<(unsigned)blocks, 128, 0, st>>>(Ns, rowptr, keys, (T *)vals, (const T *)diag, mcount, d_err);
+    csr_merge_kernel<T><<<(unsigned)blocks, 128, 0, st>>>(Ns, rowptr, fillcnt, keys, (T *)vals, (const T *)diag,
+                                                          mcount, d_err);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
 
 // Pass 3: per-row sort / term-ordered sum / diagonal add / zero drop.
-// mcount: int64[Ns] merged counts (bit 8 of d_err: row longer than 512).
-extern "C" int qs_csr_merge(int vtype, int64_t Ns, const int64_t *rowptr, uint64_t *keys, void *vals,
-                            const void *diag, int64_t *mcount, int *d_err, void *stream)
+// fillcnt: int64[Ns] entries scattered per row (the fill cursor); with a
+// diagonal array (nullable) every row range [rowptr[r], rowptr[r+1]) must
+// hold fillcnt[r] + 1 slots.  mcount: int64[Ns] merged counts.  d_err bit 8:
+// a row longer than 512 entries or without its spare slot.
+extern "C" int qs_csr_merge(int vtype, int64_t Ns, const int64_t *rowptr, const int64_t *fillcnt, uint64_t *keys,
+                            void *vals, const void *diag, int64_t *mcount, int *d_err, void *stream)
 {
-    if (Ns < 0 || !rowptr || !mcount || !d_err) return QS_ERR_ARG;
+    if (Ns < 0 || !rowptr || !fillcnt || !mcount || !d_err) return QS_ERR_ARG;
     if (Ns == 0) return QS_OK;
-    DISPATCH_VT(vtype, csr_merge_t, Ns, rowptr, keys, vals, diag, mcount, d_err, qs_stream(stream));
+    DISPATCH_VT(vtype, csr_merge_t, Ns, rowptr, fillcnt, keys, vals, diag, mcount, d_err, qs_stream(stream));
 }
 
 template <typename T>

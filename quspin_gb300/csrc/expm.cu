@@ -119,13 +119,20 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
 {
     if (*((volatile int *)&ctl->done)) return;
     const cdbl cf = coeff[j];
+    // Rows are handed out per warp (32/G consecutive rows per warp and
+    // iteration): the loop bound is warp-uniform, so every lane reaches the
+    // full-mask shuffles; groups past the last row idle.
+    constexpr int GPW = 32 / G;
     const int lane = threadIdx.x & (G - 1);
-    const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+    const int gsub = (threadIdx.x & 31) / G;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double mb = 0.0, mf = 0.0;
-    for (int64_t r = group; r < n; r += ngroups) {
-        const int64_t k0 = indptr[r], k1 = indptr[r + 1];
-        double rb = 0.0, rf = 0.0;
+    for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int64_t r = rb + gsub;
+        const bool valid = r < n;
+        const int64_t k0 = valid ? (int64_t)indptr[r] : 0, k1 = valid ? (int64_t)indptr[r + 1] : 0;
+        double rb_ = 0.0, rf = 0.0;
         for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
             cdbl acc[NB];
 #pragma unroll
@@ -145,7 +152,7 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
                     acc[b].y += __shfl_down_sync(0xffffffffu, acc[b].y, o, G);
                 }
             }
-            if (lane == 0) {
+            if (valid && lane == 0) {
 #pragma unroll
                 for (int b = 0; b < NB; b++) {
                     if (c0 + b >= nvec) break;
@@ -159,12 +166,12 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
                     cdbl f = F[e];
                     f.x += bn.x; f.y += bn.y;
                     F[e] = f;
-                    rb += cabs_(bn);
+                    rb_ += cabs_(bn);
                     rf += cabs_(f);
                 }
             }
         }
-        mb = fmax(mb, rb);
+        mb = fmax(mb, rb_);
         mf = fmax(mf, rf);
     }
     fold_max2(mb, mf, &ctl->c2, &ctl->fn);
@@ -229,7 +236,7 @@ static int pick_group_e(int64_t n, int64_t nnz)
 
 static int grid_for(int64_t n, int G)
 {
-    int64_t gpb = 256 / G;
+    int64_t gpb = 256 / G;   // rows per block per iteration
     int64_t b = (n + gpb - 1) / gpb;
     int64_t cap = (int64_t)qs_num_sms() * 8;   // 8 resident blocks of 256 threads per SM
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));

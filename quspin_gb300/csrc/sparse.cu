@@ -91,11 +91,18 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
                                                        XT *__restrict__ y, int64_t nvec, cdbl a, int overwrite)
 {
     using ACC = typename Num<XT>::acc;
+    // Rows are handed out per warp (32/G consecutive rows per warp and
+    // iteration) so the loop bound is uniform across the warp and every lane
+    // reaches the full-mask shuffles; groups past the last row idle.
+    constexpr int GPW = 32 / G;
     const int lane = threadIdx.x & (G - 1);
-    const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
-    for (int64_t r = group; r < n; r += ngroups) {
-        const int64_t k0 = indptr[r], k1 = indptr[r + 1];
+    const int gsub = (threadIdx.x & 31) / G;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int64_t r = rb + gsub;
+        const bool valid = r < n;
+        const int64_t k0 = valid ? (int64_t)indptr[r] : 0, k1 = valid ? (int64_t)indptr[r + 1] : 0;
         for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
             ACC acc[NB];
 #pragma unroll
@@ -112,7 +119,7 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
 #pragma unroll
                 for (int o = G / 2; o > 0; o >>= 1) add_to(acc[b], shfl_down(acc[b], o, G));
             }
-            if (lane == 0) {
+            if (valid && lane == 0) {
 #pragma unroll
                 for (int b = 0; b < NB; b++)
                     if (c0 + b < nvec) store_out(y, r * nvec + c0 + b, acc[b], a, overwrite);

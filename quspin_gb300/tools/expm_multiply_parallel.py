@@ -1,0 +1,265 @@
+"""``ExpmMultiplyParallel``: e^{aA} v by the truncated Taylor method on the GPU.
+
+Drop-in for QuSpin 1.0.1's ``quspin.tools.expm_multiply_parallel``
+(src/quspin/tools/evolution.py:11-16 re-exports the class whose Python body is
+docs/modules/parallel_sparse_tools/expm_multiply_parallel_core/
+expm_multiply_parallel_core.html:115-463).  Same constructor, ``set_a``,
+``dot`` and properties; the same dtype rule, tolerance (eps(dtype)/2),
+shift mu = tr(A)/n, exact 1-norm of A - mu I and (m*, s) selection.  The
+trace, 1-norm and every Taylor term run in ``csrc/sparse.cu`` /
+``csrc/expm.cu``; one ``dot`` issues s (m* + 1) + 1 launches and never
+synchronises with the host until the result is read.
+
+``precision="mixed"`` is this package's complex64 form: A's values are
+stored in float32 / complex64 and the Taylor term vectors B in complex64
+(half the bytes per term) while F, mu, the coefficients and both norms of the
+stopping test stay in double precision.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from .. import _device as D
+from .. import _lib
+from ..sparse import DeviceCSR, DeviceDIA, to_device_matrix
+from ._partition import LazyOperatorNormInfo, fragment_3_1
+
+
+def _as_device_csr(A):
+    from ..operators import hamiltonian
+    if isinstance(A, hamiltonian):
+        return A.tocsr_gpu()
+    if isinstance(A, DeviceCSR):
+        return A
+    if isinstance(A, DeviceDIA):
+        return DeviceCSR.from_scipy(A.tocsr(), A.dtype)
+    if isinstance(A, np.ndarray):
+        A = sp.csr_matrix(A)
+    return to_device_matrix(sp.csr_matrix(A))
+
+
+class ExpmMultiplyParallel:
+    """Truncated-Taylor action of e^{aA} (html :115-260)."""
+
+    def __init__(self, A, a=1.0, dtype=None, copy=False, precision="double"):
+        if np.array(a).ndim == 0:
+            self._a = a
+        else:
+            raise ValueError("a must be scalar value.")
+        if A.shape[0] != A.shape[1]:
+            raise ValueError("A must be a square matrix.")
+        self._Ad = _as_device_csr(A)
+        if copy:
+            self._Ad = DeviceCSR(self._Ad.indptr.clone(), self._Ad.indices.clone(), self._Ad.data.clone(),
+                                 self._Ad.shape, self._Ad.dtype)
+        if precision not in ("double", "mixed"):
+            raise ValueError("precision must be 'double' or 'mixed'")
+        self._precision = precision
+        Adt = self._Ad.dtype
+        a_dtype_min = np.min_scalar_type(self._a)
+        if dtype is None:
+            self._dtype = np.result_type(Adt, a_dtype_min, np.float64)
+        else:
+            min_dtype = np.result_type(Adt, a_dtype_min, np.float32)
+            if not np.can_cast(min_dtype, dtype):
+                raise ValueError("dtype not sufficient to represent a*A to at least float32 precision.")
+            self._dtype = np.dtype(dtype)
+        self._tol = np.array(np.finfo(self._dtype).eps / 2, dtype=np.finfo(self._dtype).eps.dtype)
+        n = self._Ad.shape[0]
+        tr = self._Ad.trace() if n else 0.0
+        self._mu = np.array(tr / n if n else 0.0, dtype=self._dtype)
+        self._A_1_norm = self._Ad.onenorm(-complex(self._mu)) if n else 0.0
+        self._AH = None
+        self._mixed = None
+        self._bufs = {}
+        self._calculate_partition()
+
+    @property
+    def a(self):
+        return self._a
+
+    @property
+    def A(self):
+        """Host scipy.sparse.csr_matrix copy of the exponentiated matrix."""
+        return self._Ad.tocsr()
+
+    @property
+    def A_device(self):
+        return self._Ad
+
+    @property
+    def m_star(self):
+        return self._m_star
+
+    @property
+    def s(self):
+        return self._s
+
+    def set_a(self, a, dtype=None):
+        """New scale a (html :216-260)."""
+        if np.array(a).ndim == 0:
+            self._a = a
+            a_dtype_min = np.min_scalar_type(self._a)
+            if dtype is None:
+                self._dtype = np.result_type(self._Ad.dtype, a_dtype_min, np.float64)
+            else:
+                min_dtype = np.result_type(self._Ad.dtype, a_dtype_min, np.float32)
+                if not np.can_cast(min_dtype, dtype):
+                    raise ValueError("dtype not sufficient to represent a*A to at least float32 precision.")
+                self._dtype = np.dtype(dtype)
+            self._tol = np.array(np.finfo(self._dtype).eps / 2, dtype=np.finfo(self._dtype).eps.dtype)
+            self._mu = np.array(self._mu, dtype=self._dtype)
+            self._calculate_partition()
+        else:
+            raise ValueError("expecting 'a' to be scalar.")
+
+    def set_partition(self, m_star, s):
+        """Use an externally chosen (m*, s) (the learned predictor's entry)."""
+        self._m_star, self._s = int(m_star), max(int(s), 1)
+
+    # -- (m*, s) ---------------------------------------------------------------
+    def _shifted_apply(self, conj):
+        a = complex(self._a)
+        mu = complex(self._mu)
+        if conj:
+            a, mu = np.conj(a), np.conj(mu)
+            if self._AH is None:
+                self._AH = DeviceCSR.from_scipy(self._Ad.tocsr().conj().T.tocsr(), self._Ad.dtype)
+            M = self._AH
+        else:
+            M = self._Ad
+
+        def f(v):
+            v = np.asarray(v)
+            x = D.to_device(v, np.complex128)
+            x2 = x.reshape(x.shape[0], -1).contiguous()
+            y = torch.empty_like(x2)
+            M.matvec_into(x2, y, a=a, overwrite=True)
+            y.sub_(x2, alpha=a * mu)
+            return D.to_host(y.reshape(x.shape))
+        return f
+
+    def _calculate_partition(self):
+        if np.abs(self._a) * self._A_1_norm == 0:
+            self._m_star, self._s = 0, 1
+        else:
+            self._norm_info = LazyOperatorNormInfo(self._shifted_apply(False), self._shifted_apply(True),
+                                                   self._Ad.shape[0], self._A_1_norm, self._a,
+                                                   np.dtype(np.complex128), ell=2)
+            self._m_star, self._s = fragment_3_1(self._norm_info, 1, self._tol, ell=2)
+
+    # -- application -------------------------------------------------------------
+    def _mixed_matrix(self):
+        if self._mixed is None:
+            A = self._Ad
+            vt = np.dtype(np.float32) if A.dtype.kind == "f" else np.dtype(np.complex64)
+            self._mixed = A.astype(vt)
+        return self._mixed
+
+    def _buffers(self, n, nvec, btype):
+        key = (n, nvec, btype)
+        b = self._bufs.get(key)
+        if b is None:
+            esz_dt = torch.complex128 if btype == _lib.C128 else torch.complex64
+            work = torch.empty(2 * n * nvec, dtype=esz_dt, device=D.device())
+            ctl = torch.zeros(max(_lib.load().qs_expm_ctl_bytes() // 8, 1) + 1, dtype=torch.int64,
+                              device=D.device())
+            b = (work, ctl)
+            self._bufs = {key: b}
+        return b
+
+    def run_device(self, F, tol=None, work=None):
+        """In place e^{aA} F for a complex128 device tensor F of shape (n,) or
+        (n, k).  Returns F.  No host synchronisation."""
+        n = self._Ad.shape[0]
+        nvec = 1 if F.dim() == 1 else F.shape[1]
+        tol = float(self._tol if tol is None else tol)
+        a = complex(self._a)
+        mu = complex(self._mu)
+        s, m = int(self._s), int(self._m_star)
+        mixed = self._precision == "mixed"
+        M = self._mixed_matrix() if mixed else self._Ad
+        btype = _lib.C64 if mixed else _lib.C128
+        wbuf, ctl = self._buffers(n, nvec, btype)
+        if work is not None and not mixed:
+            wbuf = work
+        ctl.zero_()
+        coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], dtype=np.complex128)
+        eta = np.exp(a * mu / s)
+        consts = D.to_device(np.concatenate([coeff, [eta, 1.0 + 0j]]).astype(np.complex128))
+        cf = consts[:max(m, 1)]
+        etap = consts[max(m, 1):max(m, 1) + 1]
+        onep = consts[max(m, 1) + 1:]
+        _lib.call("qs_expm_multiply", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
+                  D.code(M.dtype), D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, D.ptr(cf), D.ptr(etap),
+                  D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), 0, D.stream())
+        self._last_ctl = ctl
+        self._consts = consts     # keep alive until the stream reaches it
+        return F
+
+    @property
+    def terms_executed(self):
+        """Taylor terms executed by the last dot (reads the device counter)."""
+        c = getattr(self, "_last_ctl", None)
+        if c is None:
+            return 0
+        return int(c[4].item())
+
+    def dot(self, v, work_array=None, overwrite_v=False, tol=None):
+        """e^{aA} v (html :265-374); numpy in -> numpy out, CUDA tensor in ->
+        CUDA tensor out (in place when overwrite_v)."""
+        host = not D.is_device_array(v)
+        if host:
+            v = np.asarray(v)
+        if v.ndim > 2:
+            raise ValueError("array must have ndim <= 2.")
+        if v.shape[0] != self._Ad.shape[1]:
+            raise ValueError("dimension mismatch {}, {}".format(self._Ad.shape, v.shape))
+        vdt = v.dtype if host else D.np_dtype(v.dtype)
+        v_dtype = np.result_type(self._dtype, vdt)
+        if overwrite_v:
+            if v_dtype != vdt:
+                raise ValueError("if overwrite_v is True, the input array must match correct output dtype for "
+                                 "matrix multiplication.")
+            if host and not v.flags["CARRAY"]:
+                raise TypeError("input array must a contiguous and writable.")
+        if work_array is not None:
+            wsz = work_array.size if host or not D.is_device_array(work_array) else work_array.numel()
+            vsz = v.size if host else v.numel()
+            if wsz != 2 * vsz:
+                raise ValueError("work_array must have twice the number of elements as in v.")
+            wdt = work_array.dtype if not D.is_device_array(work_array) else D.np_dtype(work_array.dtype)
+            if wdt != v_dtype:
+                raise ValueError("work_array must be array of dtype which matches the result of the "
+                                 "matrix-vector multiplication.")
+        if tol is not None:
+            tol = float(np.array(tol, dtype=np.array(self._mu).real.dtype))
+        n = self._Ad.shape[0]
+        if n == 0:
+            return v if overwrite_v else v.copy() if host else v.clone()
+        if not host and v.dtype == torch.complex128 and v.is_contiguous():
+            F = v if overwrite_v else v.clone()
+            wdev = work_array.view(-1) if (D.is_device_array(work_array) and
+                                           work_array.dtype == torch.complex128) else None
+            self.run_device(F, tol=tol, work=wdev)
+            return F
+        F = D.to_device(v, np.complex128).clone()
+        self.run_device(F, tol=tol)
+        if host:
+            res = D.to_host(F)
+            res = res.astype(v_dtype) if v_dtype.kind == "c" else res.real.astype(v_dtype)
+            if overwrite_v:
+                v[...] = res
+                return v
+            return res
+        res = F if v_dtype.kind == "c" else F.real
+        res = res.to(D.torch_dtype(v_dtype))
+        if overwrite_v:
+            v.copy_(res)
+            return v
+        return res
+
+
+expm_multiply_parallel = ExpmMultiplyParallel

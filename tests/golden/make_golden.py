@@ -1,0 +1,138 @@
+"""Generates tests/golden/*.npz (run once in a container that has the
+reference checkout at /root/reference; the fixtures are committed).
+
+What runs from the reference itself:
+  * src/quspin/tools/lanczos/_lanczos_utils.py and _expm.py, imported
+    unmodified with a stand-in for numba.njit (numba is not installed);
+  * the Python body of ExpmMultiplyParallel from the Sphinx viewcode page
+    docs/modules/parallel_sparse_tools/expm_multiply_parallel_core/
+    expm_multiply_parallel_core.html (text of its <pre> block), with its four
+    native wrappers supplied by the oracle restatement (oracle/sparse_oracle.c);
+  * scipy.sparse.linalg.expm_multiply, the arbiter of the reference's own
+    tests (test/test_expm_multiply_parallel.py:65-74).
+The basis and Hamiltonian come from the oracle restatement (the reference's
+native basis core is not installable here).
+
+Usage:  python tests/golden/make_golden.py
+"""
+import html
+import importlib.util
+import os
+import re
+import sys
+import types
+
+import numpy as np
+import scipy.sparse as sp
+from scipy.sparse.linalg import expm_multiply
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = "/root/reference"
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from tests.models import chain_maps, xxz_static  # noqa: E402
+
+
+def _numba_stub():
+    def njit(*a, **k):
+        if a and callable(a[0]):
+            return a[0]
+        return lambda f: f
+    sys.modules["numba"] = types.SimpleNamespace(njit=njit)
+
+
+def reference_lanczos():
+    _numba_stub()
+    path = os.path.join(REF, "src/quspin/tools/lanczos/_lanczos_utils.py")
+    spec = importlib.util.spec_from_file_location("ref_lanczos_utils", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def reference_expm_class():
+    page = os.path.join(REF, "docs/modules/parallel_sparse_tools/expm_multiply_parallel_core/"
+                        "expm_multiply_parallel_core.html")
+    text = open(page).read()
+    src = re.search(r'<div class="highlight"><pre>(.*?)</pre>', text, re.S).group(1)
+    src = html.unescape(re.sub(r"<[^>]+>", "", src)).replace("[docs]", "")
+    src = src.replace("from .expm_multiply_parallel_wrapper import (", "from _golden_wrappers import (")
+    wr = types.ModuleType("_golden_wrappers")
+
+    def _trace(indptr, indices, data):
+        A = sp.csr_matrix((data, indices, indptr))
+        return O.csr_trace(A)
+
+    def _one_norm(indptr, indices, data, shift):
+        A = sp.csr_matrix((data, indices, indptr))
+        return O.csr_1_norm(A, shift)
+
+    def _expm(indptr, indices, data, s, m_star, tol, mu, a, v, work):
+        A = sp.csr_matrix((data, indices, indptr), shape=(v.shape[0], v.shape[0]))
+        x = np.ascontiguousarray(v, dtype=np.complex128)
+        w = np.zeros(2 * x.size, np.complex128)
+        ip, ix, dt, cp, n = O._csr_parts(A)
+        a, mu = complex(a), complex(mu)
+        eta = np.exp(a * mu / s)
+        O.lib().orc_expm_multiply(ip, ix, dt, cp, n, 1 if x.ndim == 1 else x.shape[1], int(s), int(m_star),
+                                  float(tol), mu.real, mu.imag, a.real, a.imag, eta.real, eta.imag,
+                                  x.view(np.float64).reshape(-1), w.view(np.float64).reshape(-1))
+        v[...] = x if np.iscomplexobj(v) else x.real
+
+    wr._wrapper_csr_trace = _trace
+    wr._wrapper_csr_1_norm = _one_norm
+    wr._wrapper_expm_multiply = _expm
+    wr._wrapper_expm_multiply_batch = _expm
+    sys.modules["_golden_wrappers"] = wr
+    ns = {}
+    exec(compile(src, page, "exec"), ns)
+    return ns["ExpmMultiplyParallel"]
+
+
+def main():
+    L = 20
+    m = chain_maps(L)
+    blocks = dict(kblock=(m["t"], 0), pblock=(m["p"], 0))
+    ob = O.OracleBasis(L, [(1, L // 2, 0)], pauli=0, **blocks)
+    H = sp.csr_matrix(O.make_static(ob, xxz_static(L, 1.0, 0.5), np.float64))
+    rng = np.random.default_rng(2024)
+    v = rng.normal(size=ob.Ns) + 1j * rng.normal(size=ob.Ns)
+    v /= np.linalg.norm(v)
+    v0 = np.random.default_rng(2025).normal(size=ob.Ns)
+
+    EMP = reference_expm_class()
+    np.random.seed(0)
+    ref = EMP(H, a=-1j)
+    w_ref = ref.dot(v.copy())
+    w_scipy = expm_multiply(-1j * H, v)
+
+    lz = reference_lanczos()
+    E, V, Q_T = lz.lanczos_full(H, v0, 60)
+    E_iter, V_iter = lz.lanczos_iter(H, v0, 60, return_vec_iter=False)
+
+    np.savez_compressed(os.path.join(HERE, "c1_xxz_L20.npz"), states=ob.states, norms=ob.norms,
+                        indptr=H.indptr, indices=H.indices, data=H.data, v=v, v0=v0, expm_ref=w_ref,
+                        expm_scipy=w_scipy, m_star=ref._m_star, s=ref._s, mu=complex(ref._mu),
+                        A_1_norm=ref._A_1_norm, lanczos_E=E, lanczos_iter_E=E_iter)
+
+    # the reference's random-matrix test shape (test_expm_multiply_parallel.py:52-75)
+    rs = np.random.RandomState(0)
+    N = 3500
+    A = sp.random(N, N, density=np.log(N) / N, format="csr", random_state=rs) \
+        + 1j * sp.random(N, N, density=np.log(N) / N, format="csr", random_state=rs)
+    A = sp.csr_matrix((A + A.conj().T) / 2)
+    x = rs.normal(0, 1, N) + 1j * rs.normal(0, 1, N)
+    x /= np.linalg.norm(x)
+    np.random.seed(0)
+    y_ref = EMP(A, a=-0.7j).dot(x.copy())
+    y_scipy = expm_multiply(-0.7j * A, x)
+    np.savez_compressed(os.path.join(HERE, "random_complex_N3500.npz"), indptr=A.indptr, indices=A.indices,
+                        data=A.data, x=x, expm_ref=y_ref, expm_scipy=y_scipy)
+    print("Ns", ob.Ns, "nnz", H.nnz, "m*,s", ref._m_star, ref._s, "E0", E[0],
+          "|ref-scipy|", np.abs(w_ref - w_scipy).max(), np.abs(y_ref - y_scipy).max())
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,138 @@
+"""CPU checks of the oracle (no GPU): known answers from the reference's own
+tests, invariants, and the committed golden fixtures."""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as sla
+from scipy.sparse.linalg import expm_multiply
+
+from oracle import oracle as O
+from tests.models import chain_maps, hubbard_static, square_maps, xxz_static
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# arXiv:cond-mat/0604319 Sec. III A, as quoted by test/test_FHM_energies.py:20-33
+E_PAPER = -np.array([12.0000000000000000, 11.9126285145094126, 11.8364690235642218, 11.7695877912829268,
+                     11.7104580743242632, 11.6578605150913841, 11.6108110503797608, 11.5685079573602838,
+                     11.5302924026297138])
+
+
+def test_c1_dimension_and_golden_basis():
+    m = chain_maps(20)
+    ob = O.OracleBasis(20, [(1, 10, 0)], pauli=0, kblock=(m["t"], 0), pblock=(m["p"], 0))
+    g = np.load(os.path.join(GOLD, "c1_xxz_L20.npz"))
+    assert ob.Ns == 4752
+    np.testing.assert_array_equal(ob.states, g["states"])
+    np.testing.assert_array_equal(ob.norms, g["norms"])
+    H = sp.csr_matrix(O.make_static(ob, xxz_static(20), np.float64))
+    np.testing.assert_array_equal(H.indptr, g["indptr"])
+    np.testing.assert_array_equal(H.indices, g["indices"])
+    np.testing.assert_array_equal(H.data, g["data"])
+
+
+def test_fhm_known_answers_symmetric_sector():
+    """test/test_FHM_energies_symm_adv.py: kx=ky=0 sector, advanced maps."""
+    N = 16
+    sq = square_maps(4, 4)
+    TX, TY = np.hstack((sq["tx"], sq["tx"] + N)), np.hstack((sq["ty"], sq["ty"] + N))
+    ob = O.OracleBasis(2 * N, [(2, 2, 2)], fermion=True, spinful=True, ky=(TY, 0), kx=(TX, 0))
+    Jp = [[1.0, i, TX[i]] for i in range(2 * N)] + [[1.0, i, TY[i]] for i in range(2 * N)]
+    Jm = [[-1.0, i, TX[i]] for i in range(2 * N)] + [[-1.0, i, TY[i]] for i in range(2 * N)]
+    H0 = O.make_static(ob, [["+-", Jp], ["-+", Jm]], np.float64)
+    H1 = O.make_static(ob, [["nn", [[1.0, i, i + N] for i in range(N)]]], np.float64)
+    E = [np.linalg.eigvalsh((H0 + U * H1).toarray())[0] for U in np.linspace(0.0, 4.0, 9)]
+    np.testing.assert_allclose(E, E_PAPER, atol=1e-12)
+
+
+def test_fhm_simple_symmetry_matches_advanced():
+    sq = square_maps(4, 4)
+    ob = O.OracleBasis(32, [(2, 2, 2)], fermion=True, spinful=True,
+                       kx=O.process_spinful_map(16, sq["tx"], 0), ky=O.process_spinful_map(16, sq["ty"], 0))
+    H = O.make_static(ob, hubbard_static(4, 4, 1.0, 4.0), np.float64)
+    assert abs(np.linalg.eigvalsh(H.toarray())[0] - E_PAPER[-1]) < 1e-12
+
+
+def test_sector_sums_and_spectra():
+    """test/test_sq_lat_Heis.py:19-56 on a 3x3 lattice: Ns of all momentum x
+    inversion blocks sums to the particle sector and the spectra agree."""
+    sq = square_maps(3, 3)
+    J = [[1.0, i, sq["tx"][i]] for i in range(9)] + [[1.0, i, sq["ty"][i]] for i in range(9)]
+    st = [["zz", J], ["+-", J], ["-+", J]]
+    for Nup in (3, 4):
+        full = O.OracleBasis(9, [(1, Nup, 0)], pauli=1)
+        Ef = np.linalg.eigvalsh(O.make_static(full, st, np.float64).toarray())
+        tot, Es = 0, []
+        for kx in range(3):
+            for ky in range(3):
+                b = O.OracleBasis(9, [(1, Nup, 0)], pauli=1, tx=(sq["tx"], kx), ty=(sq["ty"], ky))
+                tot += b.Ns
+                if b.Ns:
+                    Es.append(np.linalg.eigvalsh(O.make_static(b, st, np.complex128).toarray()))
+        assert tot == full.Ns
+        np.testing.assert_allclose(np.sort(np.concatenate(Es)), Ef, atol=1e-12)
+
+
+def test_oracle_expm_matches_golden_and_scipy():
+    g = np.load(os.path.join(GOLD, "c1_xxz_L20.npz"))
+    H = sp.csr_matrix((g["data"], g["indices"], g["indptr"]))
+    np.random.seed(0)
+    e = O.ExpmMultiplyParallelOracle(H, a=-1j)
+    assert (e._m_star, e._s) == (int(g["m_star"]), int(g["s"]))
+    w = e.dot(g["v"])
+    np.testing.assert_allclose(w, g["expm_ref"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(w, g["expm_scipy"], rtol=0, atol=1e-14)
+    r = np.load(os.path.join(GOLD, "random_complex_N3500.npz"))
+    A = sp.csr_matrix((r["data"], r["indices"], r["indptr"]))
+    y = O.ExpmMultiplyParallelOracle(A, a=-0.7j).dot(r["x"])
+    np.testing.assert_allclose(y, r["expm_scipy"], rtol=0, atol=1e-15)
+
+
+def test_oracle_lanczos_matches_reference_golden():
+    g = np.load(os.path.join(GOLD, "c1_xxz_L20.npz"))
+    H = sp.csr_matrix((g["data"], g["indices"], g["indptr"]))
+    E = O.lanczos_full(lambda x: H @ x, H.dtype, g["v0"], 60)[0]
+    np.testing.assert_allclose(E, g["lanczos_E"], rtol=0, atol=1e-12)
+    assert abs(E[0] - sla.eigsh(H, k=1, which="SA")[0][0]) < 1e-10
+
+
+def test_partition_restatement_matches_scipy():
+    """quspin_gb300.tools._partition restates Al-Mohy & Higham Code Fragment
+    3.1; compare with scipy's implementation, which the reference calls."""
+    from scipy.sparse.linalg._expm_multiply import LazyOperatorNormInfo as SciInfo
+    from scipy.sparse.linalg._expm_multiply import _fragment_3_1
+    from quspin_gb300.tools import _partition as P
+    rng = np.random.default_rng(0)
+    for scale in (1e-3, 0.5, 3.0, 30.0, 80.0, 400.0):
+        A = sp.random(200, 200, density=0.05, random_state=rng, format="csr") * scale
+        A = A + A.T
+        np.random.seed(5)
+        ref = _fragment_3_1(SciInfo(A, A_1_norm=sla.norm(A, 1), ell=2), 1, 2.0 ** -53, ell=2)
+        np.random.seed(5)
+        info = P.LazyOperatorNormInfo(lambda v: A @ v, lambda v: A.T @ v, 200, sla.norm(A, 1), 1.0,
+                                      np.dtype(np.float64))
+        assert P.fragment_3_1(info, 1, 2.0 ** -53, ell=2) == ref
+
+
+def test_oracle_taylor_vs_scipy_batch():
+    m = chain_maps(12)
+    ob = O.OracleBasis(12, [(1, 6, 0)], pauli=0, kblock=(m["t"], 0))
+    H = sp.csr_matrix(O.make_static(ob, xxz_static(12), np.float64))
+    rng = np.random.default_rng(1)
+    V = rng.normal(size=(ob.Ns, 5)) + 1j * rng.normal(size=(ob.Ns, 5))
+    V /= np.linalg.norm(V, axis=0)
+    W = O.ExpmMultiplyParallelOracle(H, a=-2j).dot(V)
+    np.testing.assert_allclose(W, expm_multiply(-2j * H, V), rtol=0, atol=5e-14)
+
+
+def test_op_masks_and_pauli_scaling():
+    m = chain_maps(8)
+    b0 = O.OracleBasis(8, [(1, 4, 0)], pauli=0, kblock=(m["t"], 0))
+    b1 = O.OracleBasis(8, [(1, 4, 0)], pauli=1, kblock=(m["t"], 0))
+    ME0, r0, c0 = b0.Op("+-", [3, 4], 1.0, np.float64)
+    ME1, r1, c1 = b1.Op("+-", [3, 4], 1.0, np.float64)
+    np.testing.assert_array_equal(ME1, 4 * ME0)
+    assert np.all(ME0 != 0)
+    with pytest.raises(TypeError):
+        O.make_static(O.OracleBasis(8, [(1, 4, 0)], pauli=0, kblock=(m["t"], 1)), xxz_static(8), np.float64)

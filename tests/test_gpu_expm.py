@@ -1,0 +1,139 @@
+"""GPU expm_multiply_parallel vs the oracle and scipy, following the
+reference's own checks (test/test_expm_multiply_parallel.py:9-103 and
+test/test_expm_multiply_parallel_batch.py): atol 1e-15 / 5e-15 against scipy
+for the FP64 path; a stated tolerance for the mixed (complex64) form."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+from scipy.sparse.linalg import expm_multiply
+
+from oracle import oracle as O
+from tests.models import chain_maps, xxz_static
+
+pytestmark = pytest.mark.gpu
+
+
+def _c1_like(L=14):
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    m = chain_maps(L)
+    b = spin_basis_general(L, Nup=L // 2, kblock=(m["t"], 0), pblock=(m["p"], 0), pauli=0)
+    return hamiltonian(xxz_static(L), [], basis=b, dtype=np.float64)
+
+
+def test_partition_and_shift_match_oracle(cuda):
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like()
+    A = H.tocsr()
+    for a in (-1j, -0.3j, -5j, -0.1):
+        np.random.seed(0)
+        g = ExpmMultiplyParallel(H.tocsr_gpu(), a=a)
+        np.random.seed(0)
+        o = O.ExpmMultiplyParallelOracle(A, a=a)
+        assert abs(complex(g._mu) - complex(o._mu)) < 1e-13
+        assert abs(g._A_1_norm - o._A_1_norm) < 1e-12 * o._A_1_norm
+        assert (g._m_star, g._s) == (o._m_star, o._s)
+
+
+@pytest.mark.parametrize("a", [-1j, -0.5, -5j])
+def test_expm_vs_oracle_and_scipy(cuda, a):
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like()
+    A = H.tocsr()
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=A.shape[0]) + 1j * rng.normal(size=A.shape[0])
+    v /= np.linalg.norm(v)
+    np.random.seed(1)
+    w = ExpmMultiplyParallel(H.tocsr_gpu(), a=a).dot(v)
+    np.random.seed(1)
+    wo = O.ExpmMultiplyParallelOracle(A, a=a).dot(v)
+    ws = expm_multiply(a * A, v)
+    assert np.linalg.norm(w - wo) <= 1e-12 * np.linalg.norm(wo)
+    np.testing.assert_allclose(w, ws, rtol=0, atol=1e-13)
+
+
+def test_expm_batch(cuda):
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like(12)
+    A = H.tocsr()
+    rng = np.random.default_rng(8)
+    V = rng.normal(size=(A.shape[0], 10)) + 1j * rng.normal(size=(A.shape[0], 10))
+    V /= np.linalg.norm(V, axis=0)
+    W = ExpmMultiplyParallel(A, a=-0.7j).dot(V)
+    Ws = expm_multiply(-0.7j * A, V)
+    np.testing.assert_allclose(W, Ws, rtol=0, atol=5e-14)
+
+
+def test_reference_random_matrices(cuda):
+    """test_expm_multiply_parallel.py:52-75: random complex sparse N=3500,
+    density log N / N, compared with scipy at atol 1e-15 (after scaling by the
+    state norm); and the int8 matrix with a = -0.01j (:78-103)."""
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    rs = np.random.RandomState(0)
+    N = 3500
+    for _ in range(3):
+        A = sp.random(N, N, density=np.log(N) / N, format="csr", random_state=rs) \
+            + 1j * sp.random(N, N, density=np.log(N) / N, format="csr", random_state=rs)
+        A = (A + A.conj().T) / 2
+        v = rs.normal(0, 1, N) + 1j * rs.normal(0, 1, N)
+        v /= np.linalg.norm(v)
+        t = rs.uniform(-1, 1)
+        w = ExpmMultiplyParallel(A, a=-1j * t).dot(v)
+        ws = expm_multiply(-1j * t * A, v)
+        np.testing.assert_allclose(w, ws, rtol=0, atol=1e-14)
+    A = sp.random(N, N, density=np.log(N) / N, format="csr", random_state=rs)
+    A.data = (A.data * 100).astype(np.int8)
+    A = sp.csr_matrix(A, dtype=np.int8)
+    v = rs.normal(0, 1, N) + 1j * rs.normal(0, 1, N)
+    v /= np.linalg.norm(v)
+    w = ExpmMultiplyParallel(A, a=-0.01j, dtype=np.complex128).dot(v)
+    ws = expm_multiply(-0.01j * A.astype(np.float64), v)
+    np.testing.assert_allclose(w, ws, rtol=0, atol=1e-14)
+
+
+def test_imaginary_time_real_dtype(cuda):
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like(12)
+    A = H.tocsr()
+    rng = np.random.default_rng(9)
+    v = rng.normal(size=A.shape[0])
+    w = ExpmMultiplyParallel(A, a=-0.5).dot(v)
+    assert w.dtype == np.float64
+    ws = expm_multiply(-0.5 * A, v)
+    assert np.linalg.norm(w - ws) <= 1e-13 * np.linalg.norm(ws)
+
+
+def test_overwrite_and_device_operands(cuda):
+    import torch
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like(12)
+    A = H.tocsr()
+    rng = np.random.default_rng(10)
+    v = rng.normal(size=A.shape[0]) + 1j * rng.normal(size=A.shape[0])
+    op = ExpmMultiplyParallel(H.tocsr_gpu(), a=-2j)
+    ref = expm_multiply(-2j * A, v)
+    vd = torch.tensor(v, device="cuda")
+    r = op.dot(vd, overwrite_v=True)
+    assert r.data_ptr() == vd.data_ptr()
+    np.testing.assert_allclose(vd.cpu().numpy(), ref, rtol=0, atol=1e-13)
+    vv = v.copy()
+    op.dot(vv, overwrite_v=True)
+    np.testing.assert_allclose(vv, ref, rtol=0, atol=1e-13)
+    with pytest.raises(ValueError):
+        op.dot(v.real.copy(), overwrite_v=True)
+    with pytest.raises(ValueError):
+        op.dot(v, work_array=np.zeros(3, np.complex128))
+    op.set_a(-1j)
+    np.testing.assert_allclose(op.dot(v), expm_multiply(-1j * A, v), rtol=0, atol=1e-13)
+
+
+def test_mixed_precision_error(cuda):
+    """complex64 bulk apply with FP64 accumulation: relative state error vs
+    the FP64 result stays below 1e-6 at t = 1 (stated tolerance of the form)."""
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like(14)
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=H.Ns) + 1j * rng.normal(size=H.Ns)
+    v /= np.linalg.norm(v)
+    w64 = ExpmMultiplyParallel(H.tocsr_gpu(), a=-1j).dot(v)
+    w32 = ExpmMultiplyParallel(H.tocsr_gpu(), a=-1j, precision="mixed").dot(v)
+    assert np.linalg.norm(w32 - w64) / np.linalg.norm(w64) < 1e-6
