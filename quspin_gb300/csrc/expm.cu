@@ -109,7 +109,30 @@ __device__ __forceinline__ bool last_block(ExpmCtl *ctl)
     return is_last;
 }
 
-template <typename DT, typename BT, typename IT, int G, int NB>
+template <typename T> __device__ __forceinline__ T st_ld(const T *p) { return __ldcs(p); }
+template <> __device__ __forceinline__ cdbl st_ld<cdbl>(const cdbl *p)
+{
+    double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    return cdbl{v.x, v.y};
+}
+template <> __device__ __forceinline__ cflt st_ld<cflt>(const cflt *p)
+{
+    float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    return cflt{v.x, v.y};
+}
+__device__ __forceinline__ double wid(double v) { return v; }
+__device__ __forceinline__ double wid(float v) { return (double)v; }
+__device__ __forceinline__ cdbl wid(cdbl v) { return v; }
+__device__ __forceinline__ cdbl wid(cflt v) { return cdbl{(double)v.x, (double)v.y}; }
+template <typename T> __device__ __forceinline__ T zro();
+template <> __device__ __forceinline__ double zro<double>() { return 0.0; }
+template <> __device__ __forceinline__ float zro<float>() { return 0.0f; }
+template <> __device__ __forceinline__ cdbl zro<cdbl>() { return cdbl{0.0, 0.0}; }
+template <> __device__ __forceinline__ cflt zro<cflt>() { return cflt{0.0f, 0.0f}; }
+
+// G lanes per row, U independent entries per lane per step, NB right-hand
+// sides per pass (see csrc/sparse.cu for the row hand-out rule).
+template <typename DT, typename BT, typename IT, int G, int NB, int U>
 __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *__restrict__ indptr,
                                                           const int32_t *__restrict__ indices,
                                                           const DT *__restrict__ data, const BT *__restrict__ Bin,
@@ -137,12 +160,24 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
             cdbl acc[NB];
 #pragma unroll
             for (int b = 0; b < NB; b++) acc[b] = cdbl{0.0, 0.0};
-            for (int64_t k = k0 + lane; k < k1; k += G) {
-                const int64_t col = __ldg(indices + k);
-                const auto d = DLoad<DT>::ld(data, k);
+            for (int64_t k = k0 + lane; k < k1; k += G * U) {
+                int64_t col[U];
+                DT d[U];
 #pragma unroll
-                for (int b = 0; b < NB; b++)
-                    if (c0 + b < nvec) madd(acc[b], d, BLoad<BT>::ld(Bin, col * nvec + c0 + b));
+                for (int u = 0; u < U; u++) {
+                    const int64_t kk = k + u * G;
+                    const bool in = kk < k1;
+                    col[u] = in ? (int64_t)st_ld(indices + kk) : 0;
+                    d[u] = in ? st_ld(data + kk) : zro<DT>();
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    if (k + u * G < k1) {
+#pragma unroll
+                        for (int b = 0; b < NB; b++)
+                            if (c0 + b < nvec) madd(acc[b], wid(d[u]), BLoad<BT>::ld(Bin, col[u] * nvec + c0 + b));
+                    }
+                }
             }
 #pragma unroll
             for (int b = 0; b < NB; b++) {
@@ -228,28 +263,28 @@ __global__ void __launch_bounds__(256) taylor_rescale_kernel(int64_t n, int64_t 
 static int pick_group_e(int64_t n, int64_t nnz)
 {
     double avg = n > 0 ? (double)nnz / (double)n : 1.0;
-    if (avg >= 24) return 32;
-    if (avg >= 12) return 16;
-    if (avg >= 6) return 8;
-    return 4;
+    int g = 2;
+    while (g < 32 && g * 8 < avg) g <<= 1;
+    return g;
 }
 
 static int grid_for(int64_t n, int G)
 {
     int64_t gpb = 256 / G;   // rows per block per iteration
     int64_t b = (n + gpb - 1) / gpb;
-    int64_t cap = (int64_t)qs_num_sms() * 8;   // 8 resident blocks of 256 threads per SM
+    int64_t cap = (int64_t)qs_num_sms() * 16;
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-template <typename DT, typename BT, typename IT, int NB>
-static int term_launch(int64_t n, int64_t nnz, const void *indptr, const int32_t *indices, const void *data,
-                       const void *Bin, void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j,
-                       double tol, ExpmCtl *ctl, int G, cudaStream_t st)
+template <typename DT, typename BT, typename IT, int NB, int U>
+static int term_launch(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *Bin,
+                       void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j, double tol, ExpmCtl *ctl,
+                       int G, cudaStream_t st)
 {
     int blocks = grid_for(n, G);
-#define L_(GG) taylor_term_kernel<DT, BT, IT, GG, NB><<<blocks, 256, 0, st>>>(n, (const IT *)indptr, indices, (const DT *)data, (const BT *)Bin, (BT *)Bout, F, nvec, mu, coeff, j, tol, ctl)
+#define L_(GG) taylor_term_kernel<DT, BT, IT, GG, NB, U><<<blocks, 256, 0, st>>>(n, (const IT *)indptr, indices, (const DT *)data, (const BT *)Bin, (BT *)Bout, F, nvec, mu, coeff, j, tol, ctl)
     switch (G) {
+    case 2: L_(2); break;
     case 4: L_(4); break;
     case 8: L_(8); break;
     case 16: L_(16); break;
@@ -261,37 +296,46 @@ static int term_launch(int64_t n, int64_t nnz, const void *indptr, const int32_t
 }
 
 template <typename DT, typename BT, typename IT>
-static int term_nb(int64_t n, int64_t nnz, const void *indptr, const int32_t *indices, const void *data,
-                   const void *Bin, void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j, double tol,
-                   ExpmCtl *ctl, int G, cudaStream_t st)
+static int term_nb(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *Bin,
+                   void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j, double tol, ExpmCtl *ctl,
+                   int G, int U, cudaStream_t st)
 {
-    if (nvec == 1) return term_launch<DT, BT, IT, 1>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
-    if (nvec == 2) return term_launch<DT, BT, IT, 2>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
-    if (nvec <= 4) return term_launch<DT, BT, IT, 4>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
-    return term_launch<DT, BT, IT, 8>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    if (nvec == 1) {
+        if (U >= 4) return term_launch<DT, BT, IT, 1, 4>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+        if (U == 2) return term_launch<DT, BT, IT, 1, 2>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+        return term_launch<DT, BT, IT, 1, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    }
+    if (nvec == 2) return term_launch<DT, BT, IT, 2, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    if (nvec <= 4) return term_launch<DT, BT, IT, 4, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    return term_launch<DT, BT, IT, 8, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
 }
 
 template <typename DT, typename BT>
-static int term_idx(int idx64, int64_t n, int64_t nnz, const void *indptr, const int32_t *indices, const void *data,
+static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *indices, const void *data,
                     const void *Bin, void *Bout, cdbl *F, int64_t nvec, cdbl mu, const cdbl *coeff, int j, double tol,
-                    ExpmCtl *ctl, int G, cudaStream_t st)
+                    ExpmCtl *ctl, int G, int U, cudaStream_t st)
 {
-    if (idx64) return term_nb<DT, BT, int64_t>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
-    return term_nb<DT, BT, int32_t>(n, nnz, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, st);
+    if (idx64) return term_nb<DT, BT, int64_t>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, 1, st);
+    return term_nb<DT, BT, int32_t>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, U, st);
 }
 
 // One Taylor term (see file header).  dtype: value type of A (QS_F64,
 // QS_C128, QS_F32, QS_C64); btype: storage of B (QS_C128 or QS_C64); F is
 // complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
-// ctl: device control block (qs_expm_ctl_bytes()).
+// ctl: device control block (qs_expm_ctl_bytes()).  group: launch shape,
+// G | (U << 8) (G lanes per row 2..32, U = 1, 2, 4 entries in flight per lane);
+// 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                               const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
                               int64_t nvec, double mu_re, double mu_im, const void *coeff, int j, double tol,
                               void *ctl, int group, void *stream)
 {
     if (n < 1 || nvec < 1 || !indptr || !Bin || !Bout || !F || !coeff || !ctl || j < 0) return QS_ERR_ARG;
-    int G = group > 0 ? group : pick_group_e(n, nnz);
-    if (G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
+    int G = group > 0 ? (group & 0xff) : pick_group_e(n, nnz);
+    int U = group > 0 ? ((group >> 8) & 0xff) : 2;
+    if (U < 1) U = 1;
+    if (G != 2 && G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
+    if (U != 1 && U != 2 && U != 4) return QS_ERR_ARG;
     cdbl mu{mu_re, mu_im};
     cudaStream_t st = qs_stream(stream);
     ExpmCtl *c = reinterpret_cast<ExpmCtl *>(ctl);
@@ -299,15 +343,15 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
     if (btype == QS_C128) {
         switch (dtype) {
-        case QS_F64: return term_idx<double, cdbl>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
-        case QS_C128: return term_idx<cdbl, cdbl>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        case QS_F64: return term_idx<double, cdbl>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
+        case QS_C128: return term_idx<cdbl, cdbl>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
         default: return QS_ERR_ARG;
         }
     } else if (btype == QS_C64) {
         switch (dtype) {
-        case QS_F32: return term_idx<float, cflt>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
-        case QS_C64: return term_idx<cflt, cflt>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
-        case QS_F64: return term_idx<double, cflt>(idx64, n, nnz, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, st);
+        case QS_F32: return term_idx<float, cflt>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
+        case QS_C64: return term_idx<cflt, cflt>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
+        case QS_F64: return term_idx<double, cflt>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
         default: return QS_ERR_ARG;
         }
     }

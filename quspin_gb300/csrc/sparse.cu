@@ -84,16 +84,40 @@ __device__ __forceinline__ void store_out(cflt *y, int64_t i, cdbl acc, cdbl a, 
     else { cflt o = y[i]; y[i] = cflt{(float)((double)o.x + vr), (float)((double)o.y + vi)}; }
 }
 
-template <typename DT, typename XT, typename IT, int G, int NB>
+template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+template <> __device__ __forceinline__ cdbl ld_stream<cdbl>(const cdbl *p)
+{
+    double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    return cdbl{v.x, v.y};
+}
+template <> __device__ __forceinline__ cflt ld_stream<cflt>(const cflt *p)
+{
+    float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    return cflt{v.x, v.y};
+}
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return (double)v; }
+__device__ __forceinline__ cdbl widen(cdbl v) { return v; }
+__device__ __forceinline__ cdbl widen(cflt v) { return cdbl{(double)v.x, (double)v.y}; }
+template <typename T> __device__ __forceinline__ T zero_of();
+template <> __device__ __forceinline__ double zero_of<double>() { return 0.0; }
+template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
+template <> __device__ __forceinline__ cdbl zero_of<cdbl>() { return cdbl{0.0, 0.0}; }
+template <> __device__ __forceinline__ cflt zero_of<cflt>() { return cflt{0.0f, 0.0f}; }
+
+// G lanes per row, U independent entries per lane per step (more loads in
+// flight), NB right-hand sides per pass.  Rows are handed out per warp (32/G
+// consecutive rows per warp and iteration) so the loop bound is uniform across
+// the warp and every lane reaches the full-mask shuffles; groups past the last
+// row idle.  Matrix streams are read with evict-first hints so the gathered
+// vector keeps its place in L2.
+template <typename DT, typename XT, typename IT, int G, int NB, int U>
 __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__restrict__ indptr,
                                                        const int32_t *__restrict__ indices,
                                                        const DT *__restrict__ data, const XT *__restrict__ x,
                                                        XT *__restrict__ y, int64_t nvec, cdbl a, int overwrite)
 {
     using ACC = typename Num<XT>::acc;
-    // Rows are handed out per warp (32/G consecutive rows per warp and
-    // iteration) so the loop bound is uniform across the warp and every lane
-    // reaches the full-mask shuffles; groups past the last row idle.
     constexpr int GPW = 32 / G;
     const int lane = threadIdx.x & (G - 1);
     const int gsub = (threadIdx.x & 31) / G;
@@ -107,12 +131,24 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
             ACC acc[NB];
 #pragma unroll
             for (int b = 0; b < NB; b++) set_zero(acc[b]);
-            for (int64_t k = k0 + lane; k < k1; k += G) {
-                const int64_t col = __ldg(indices + k);
-                const auto d = Num<DT>::ld(data, k);
+            for (int64_t k = k0 + lane; k < k1; k += G * U) {
+                int64_t col[U];
+                DT d[U];
 #pragma unroll
-                for (int b = 0; b < NB; b++)
-                    if (c0 + b < nvec) fma_acc(acc[b], d, Num<XT>::ld(x, col * nvec + c0 + b));
+                for (int u = 0; u < U; u++) {
+                    const int64_t kk = k + u * G;
+                    const bool in = kk < k1;
+                    col[u] = in ? (int64_t)ld_stream(indices + kk) : 0;
+                    d[u] = in ? ld_stream(data + kk) : zero_of<DT>();
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    if (k + u * G < k1) {
+#pragma unroll
+                        for (int b = 0; b < NB; b++)
+                            if (c0 + b < nvec) fma_acc(acc[b], widen(d[u]), Num<XT>::ld(x, col[u] * nvec + c0 + b));
+                    }
+                }
             }
 #pragma unroll
             for (int b = 0; b < NB; b++) {
@@ -128,27 +164,28 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
     }
 }
 
+// Lanes per row from the mean row length: about eight entries per lane.
 static int pick_group(int64_t n, int64_t nnz)
 {
     double avg = n > 0 ? (double)nnz / (double)n : 1.0;
-    if (avg >= 24) return 32;
-    if (avg >= 12) return 16;
-    if (avg >= 6) return 8;
-    return 4;
+    int g = 2;
+    while (g < 32 && g * 8 < avg) g <<= 1;
+    return g;
 }
 
-template <typename DT, typename XT, typename IT, int NB>
-static int spmm_launch_nb(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *x,
+template <typename DT, typename XT, typename IT, int NB, int U>
+static int spmm_launch_gu(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *x,
                           void *y, int64_t nvec, cdbl a, int overwrite, int G, cudaStream_t st)
 {
     int threads = 256;
     int64_t groups_per_block = threads / G;
     int64_t blocks = (n + groups_per_block - 1) / groups_per_block;
-    int64_t cap = (int64_t)qs_num_sms() * 32;
+    int64_t cap = (int64_t)qs_num_sms() * 16;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-#define L_(GG) csr_spmm_kernel<DT, XT, IT, GG, NB><<<(unsigned)blocks, threads, 0, st>>>(n, (const IT *)indptr, indices, (const DT *)data, (const XT *)x, (XT *)y, nvec, a, overwrite)
+#define L_(GG) csr_spmm_kernel<DT, XT, IT, GG, NB, U><<<(unsigned)blocks, threads, 0, st>>>(n, (const IT *)indptr, indices, (const DT *)data, (const XT *)x, (XT *)y, nvec, a, overwrite)
     switch (G) {
+    case 2: L_(2); break;
     case 4: L_(4); break;
     case 8: L_(8); break;
     case 16: L_(16); break;
@@ -161,28 +198,33 @@ static int spmm_launch_nb(int64_t n, const void *indptr, const int32_t *indices,
 
 template <typename DT, typename XT, typename IT>
 static int spmm_launch(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *x,
-                       void *y, int64_t nvec, cdbl a, int overwrite, int G, cudaStream_t st)
+                       void *y, int64_t nvec, cdbl a, int overwrite, int G, int U, cudaStream_t st)
 {
-    if (nvec == 1) return spmm_launch_nb<DT, XT, IT, 1>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-    if (nvec == 2) return spmm_launch_nb<DT, XT, IT, 2>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-    if (nvec <= 4) return spmm_launch_nb<DT, XT, IT, 4>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-    return spmm_launch_nb<DT, XT, IT, 8>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+    if (nvec == 1) {
+        if (U >= 4) return spmm_launch_gu<DT, XT, IT, 1, 4>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+        if (U == 2) return spmm_launch_gu<DT, XT, IT, 1, 2>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+        return spmm_launch_gu<DT, XT, IT, 1, 1>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+    }
+    if (nvec == 2) return spmm_launch_gu<DT, XT, IT, 2, 1>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+    if (nvec <= 4) return spmm_launch_gu<DT, XT, IT, 4, 1>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+    return spmm_launch_gu<DT, XT, IT, 8, 1>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
 }
 
 template <typename DT, typename XT>
 static int spmm_idx(int idx64, int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *x,
-                    void *y, int64_t nvec, cdbl a, int overwrite, int G, cudaStream_t st)
+                    void *y, int64_t nvec, cdbl a, int overwrite, int G, int U, cudaStream_t st)
 {
-    if (idx64) return spmm_launch<DT, XT, int64_t>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-    return spmm_launch<DT, XT, int32_t>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+    if (idx64) return spmm_launch<DT, XT, int64_t>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, 1, st);
+    return spmm_launch<DT, XT, int32_t>(n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
 }
 
 // y = a * A x (overwrite) or y += a * A x, for a CSR matrix with int32/int64
 // indptr (idx64), int32 indices, value type dtype and vector type xtype
 // (QS_F32/F64/C64/C128).  x, y: [n, nvec] C order.  Supported pairs: the
 // vector type is the result type (complex if either is complex; the value
-// precision never exceeds the vector precision's partner).  group: lanes per
-// row (0 = pick from nnz/n).
+// precision never exceeds the vector precision's partner).  group: launch
+// shape, G | (U << 8) with G lanes per row (2..32) and U in-flight entries per
+// lane (1, 2, 4); 0 picks G from nnz/n and U = 2.
 extern "C" int qs_csr_matvec(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                              const void *data, int dtype, const void *x, int xtype, void *y, int64_t nvec,
                              double a_re, double a_im, int overwrite, int group, void *stream)
@@ -190,28 +232,31 @@ extern "C" int qs_csr_matvec(int64_t n, int64_t nnz, const void *indptr, int idx
     if (n < 0 || nvec < 1 || (n > 0 && (!indptr || !x || !y))) return QS_ERR_ARG;
     if (n == 0) return QS_OK;
     cdbl a{a_re, a_im};
-    int G = group > 0 ? group : pick_group(n, nnz);
-    if (G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
+    int G = group > 0 ? (group & 0xff) : pick_group(n, nnz);
+    int U = group > 0 ? ((group >> 8) & 0xff) : 2;
+    if (U < 1) U = 1;
+    if (G != 2 && G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
+    if (U != 1 && U != 2 && U != 4) return QS_ERR_ARG;
     cudaStream_t st = qs_stream(stream);
     bool xc = xtype == QS_C64 || xtype == QS_C128;
     if (!xc && a_im != 0.0) return QS_ERR_ARG;
     switch (xtype) {
     case QS_F64:
-        if (dtype == QS_F64) return spmm_idx<double, double>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-        if (dtype == QS_F32) return spmm_idx<float, double>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+        if (dtype == QS_F64) return spmm_idx<double, double>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_F32) return spmm_idx<float, double>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     case QS_F32:
-        if (dtype == QS_F32) return spmm_idx<float, float>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+        if (dtype == QS_F32) return spmm_idx<float, float>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     case QS_C128:
-        if (dtype == QS_F64) return spmm_idx<double, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-        if (dtype == QS_C128) return spmm_idx<cdbl, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-        if (dtype == QS_F32) return spmm_idx<float, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-        if (dtype == QS_C64) return spmm_idx<cflt, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+        if (dtype == QS_F64) return spmm_idx<double, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_C128) return spmm_idx<cdbl, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_F32) return spmm_idx<float, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_C64) return spmm_idx<cflt, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     case QS_C64:
-        if (dtype == QS_F32) return spmm_idx<float, cflt>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
-        if (dtype == QS_C64) return spmm_idx<cflt, cflt>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, st);
+        if (dtype == QS_F32) return spmm_idx<float, cflt>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_C64) return spmm_idx<cflt, cflt>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     default:
         return QS_ERR_ARG;

@@ -67,11 +67,15 @@ class DeviceCSR:
             return self
         return DeviceCSR(self.indptr, self.indices, self.data.to(D.torch_dtype(dtype)), self.shape, dtype)
 
-    def matvec_into(self, x, y, a=1.0, overwrite=True, group=0):
-        """y (=|+=) a * A x on device tensors of the result dtype."""
+    def matvec_into(self, x, y, a=1.0, overwrite=True, group=None):
+        """y (=|+=) a * A x on device tensors of the result dtype.  group:
+        launch shape code (None: the autotuned one for this matrix)."""
         n = self.shape[0]
         nvec = 1 if x.dim() == 1 else x.shape[1]
         xt = D.np_dtype(x.dtype)
+        if group is None:
+            from .tune import tune_spmv
+            group = tune_spmv(self, nvec, xt)
         a = complex(a)
         _lib.call("qs_csr_matvec", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
                   D.ptr(self.data), D.code(self.dtype), D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,

@@ -192,9 +192,11 @@ class ExpmMultiplyParallel:
         cf = consts[:max(m, 1)]
         etap = consts[max(m, 1):max(m, 1) + 1]
         onep = consts[max(m, 1) + 1:]
+        from ..tune import tune_taylor
+        group = tune_taylor(M, nvec, btype)
         _lib.call("qs_expm_multiply", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
                   D.code(M.dtype), D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, D.ptr(cf), D.ptr(etap),
-                  D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), 0, D.stream())
+                  D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), group, D.stream())
         self._last_ctl = ctl
         self._consts = consts     # keep alive until the stream reaches it
         return F

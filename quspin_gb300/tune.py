@@ -1,0 +1,99 @@
+"""Launch-shape autotuner for the CSR kernels.
+
+The SpMV and Taylor-term kernels take a launch shape (G lanes per row,
+U entries in flight per lane).  The best shape depends on the row-length
+distribution and on how the gathers of the vector spread over L2, so it is
+measured: a handful of candidate shapes around the nnz/row heuristic are timed
+with CUDA events on the actual matrix and the fastest is kept on the matrix
+object.  Matrices smaller than ``MIN_ROWS`` keep the heuristic shape.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _device as D
+from . import _lib
+
+MIN_ROWS = 65536
+
+
+def encode(G, U):
+    return int(G) | (int(U) << 8)
+
+
+def _candidates(n, nnz, nvec):
+    avg = nnz / max(n, 1)
+    g = 2
+    while g < 32 and g * 8 < avg:
+        g <<= 1
+    Gs = sorted({max(2, g // 2), g, min(32, g * 2)})
+    Us = (1, 2, 4) if nvec == 1 else (1,)
+    return [(G, U) for G in Gs for U in Us]
+
+
+def _time(fn, reps=5):
+    st = torch.cuda.current_stream()
+    for _ in range(2):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        fn()
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def tune_spmv(M, nvec=1, xdtype=np.complex128):
+    """Fastest launch code for M.matvec_into with nvec columns of xdtype."""
+    key = ("spmv", nvec, np.dtype(xdtype).str)
+    cache = M.__dict__.setdefault("_tuned", {})
+    if key in cache:
+        return cache[key]
+    n = M.shape[0]
+    if n < MIN_ROWS or getattr(M, "idx64", 0):
+        cache[key] = 0
+        return 0
+    shape = (n,) if nvec == 1 else (n, nvec)
+    x = torch.ones(shape, dtype=D.torch_dtype(xdtype), device=D.device())
+    y = torch.empty_like(x)
+    best, best_t = 0, None
+    for G, U in _candidates(n, M.nnz, nvec):
+        code = encode(G, U)
+        t = _time(lambda: M.matvec_into(x, y, group=code))
+        if best_t is None or t < best_t:
+            best, best_t = code, t
+    cache[key] = best
+    return best
+
+
+def tune_taylor(M, nvec, btype):
+    """Fastest launch code for the fused Taylor term on M (stopping test off)."""
+    key = ("taylor", nvec, btype)
+    cache = M.__dict__.setdefault("_tuned", {})
+    if key in cache:
+        return cache[key]
+    n = M.shape[0]
+    if n < MIN_ROWS or getattr(M, "idx64", 0):
+        cache[key] = 0
+        return 0
+    bdt = torch.complex128 if btype == _lib.C128 else torch.complex64
+    b0 = torch.ones(n * nvec, dtype=bdt, device=D.device())
+    b1 = torch.empty_like(b0)
+    F = torch.zeros(n * nvec, dtype=torch.complex128, device=D.device())
+    ctl = torch.zeros(6, dtype=torch.int64, device=D.device())
+    coeff = torch.tensor([1e-3 + 0j], dtype=torch.complex128, device=D.device())
+    best, best_t = 0, None
+    for G, U in _candidates(n, M.nnz, nvec):
+        code = encode(G, U)
+
+        def run():
+            _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
+                      D.code(M.dtype), D.ptr(b0), D.ptr(b1), btype, D.ptr(F), nvec, 0.0, 0.0, D.ptr(coeff), 0, 0.0,
+                      D.ptr(ctl), code, D.stream())
+        t = _time(run)
+        if best_t is None or t < best_t:
+            best, best_t = code, t
+    cache[key] = best
+    return best
