@@ -132,6 +132,21 @@ int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, co
                      double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
                      void *d_work, int btype, void *d_ctl, int group, void *stream);
 
+/* ---- e^{aA} v without any device allocation.  No counterpart in the
+ * reference: this entry point exists for callers that cannot allocate GPU
+ * memory (a host application or plugin framework that owns the device memory
+ * budget, or a time-stepping loop that must not synchronise on cudaMalloc).
+ * Same arithmetic as qs_expm_multiply with complex128 Taylor buffers; its
+ * scratch is a static device array in the library (about 32 MiB per GPU, kept
+ * until exit).  Limits: n * nvec <= qs_expm_noalloc_max_elems() (1,048,576)
+ * and m_star <= 64, else -5.  The first call on a device looks up the array's
+ * device address; make it before capturing work.  Calls that overlap on the
+ * GPU share the scratch and race; serialise them. ------------------------- */
+int64_t qs_expm_noalloc_max_elems(void);
+int qs_expm_multiply_noalloc(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                             const void *d_data, int dtype, void *d_F, int64_t nvec, int s, int m_star, double tol,
+                             double mu_re, double mu_im, double a_re, double a_im, int group, void *stream);
+
 /* ---- Lanczos recurrence steps: lanczos_full / lanczos_iter
  * (src/quspin/tools/lanczos/_lanczos_utils.py:158-204, :283-311), the
  * optional full reorthogonalisation, and lin_comb_Q_T (:366-425).  Vectors
