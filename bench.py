@@ -74,7 +74,7 @@ def peak_hbm():
 def profile_traffic():
     """dram bytes per launch of the Taylor-term kernel from the committed ncu
     summary (a 'traffic_bytes_per_launch_full: <int>' line), else None."""
-    p = os.path.join(ROOT, "profiles", "taylor_term_j1j2_L32.md")
+    p = os.path.join(ROOT, "profiles", "taylor_term_j1j2.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -351,6 +351,91 @@ def run_ours(args, rank, ws):
         print(json.dumps(out))
 
 
+def ising_sector_mats(L, hx=0.9, hz=0.5):
+    """All momentum sectors of the mixed-field Ising chain, reflection
+    resolved at k = 0 and k = L/2 (26 blocks at L = 24)."""
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    s_ = np.arange(L)
+    t, p = (s_ + 1) % L, s_[::-1].copy()
+    static = [["zz", [[-1.0, i, (i + 1) % L] for i in range(L)]], ["x", [[-hx, i] for i in range(L)]],
+              ["z", [[-hz, i] for i in range(L)]]]
+    mats = []
+    for k in range(L):
+        for pq in ((0, 1) if k in (0, L // 2) else (None,)):
+            blocks = dict(kblock=(t, k))
+            if pq is not None:
+                blocks["pblock"] = (p, pq)
+            b = spin_basis_general(L, **blocks)
+            dt = np.float64 if k in (0, L // 2) else np.complex128
+            mats.append(hamiltonian(static, [], basis=b, dtype=dt).tocsr_gpu())
+    return mats
+
+
+def run_sectors(args):
+    """Many-sector workload: every momentum block of the L=24 mixed-field
+    Ising chain, 8 states per block (208 evolutions), t = 2.  Plain per-block
+    FP64 loop vs one stacked graph-captured launch sequence (FP64 and mixed)."""
+    import torch
+    from quspin_gb300.tools import ExpmMultiplyParallel, MultiSectorExpm
+    L, k, T = args.L if args.L != 32 else 24, 8, 2.0
+    t0 = time.perf_counter()
+    mats = ising_sector_mats(L)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    blocks = []
+    for M in mats:
+        V = rng.normal(size=(M.shape[0], k)) + 1j * rng.normal(size=(M.shape[0], k))
+        blocks.append(torch.tensor(V / np.linalg.norm(V, axis=0), dtype=torch.complex128, device="cuda"))
+    st = torch.cuda.current_stream()
+    ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    # plain per-block FP64 loop
+    plain = [ExpmMultiplyParallel(M, a=-1j * T) for M in mats]
+    outs = [None] * len(mats)
+
+    def plain_step():
+        for i, (op, V) in enumerate(zip(plain, blocks)):
+            outs[i] = op.dot(V)
+    for _ in range(args.warmup):
+        plain_step()
+    e0, e1 = ev()
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(args.steps):
+        plain_step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) / 1e3 / args.steps
+    ref = [o.clone() for o in outs]
+    res = {}
+    for prec in ("double", "mixed"):
+        ms = MultiSectorExpm(mats, a=-1j * T, nvec=k, precision=prec)
+        for _ in range(args.warmup):
+            ms.load(blocks)
+            ms.run_device()
+        torch.cuda.synchronize()
+        e0, e1 = ev()
+        e0.record(st)
+        for _ in range(args.steps):
+            ms.load(blocks)
+            ms.run_device()
+        e1.record(st)
+        torch.cuda.synchronize()
+        tt = e0.elapsed_time(e1) / 1e3 / args.steps
+        got = ms.blocks(host=False)
+        num = sum(float(torch.linalg.vector_norm(a - b) ** 2) for a, b in zip(got, ref)) ** 0.5
+        den = sum(float(torch.linalg.vector_norm(b) ** 2) for b in ref) ** 0.5
+        res[prec] = {"evolutions_per_s": len(mats) * k / tt, "s_per_step": tt, "rel_state_error_vs_fp64": num / den,
+                     "m_star": ms.m_star, "s": ms.s, "sector_terms": ms.terms_executed}
+    out = {"metric": "expm_multiply evolutions/s", "value": res["mixed"]["evolutions_per_s"], "unit": "evolutions/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "workload": "ising_L{}_all_k_sectors_8_states_t2".format(L), "blocks": len(mats),
+           "dims": [M.shape[0] for M in mats], "build_s": round(t_build, 3),
+           "plain_fp64_per_block_loop": {"evolutions_per_s": len(mats) * k / t_plain, "s_per_step": t_plain},
+           "stacked_fp64": res["double"], "stacked_mixed": res["mixed"]}
+    print(json.dumps(out))
+
+
 def run_reference(args, rank, ws):
     """The reference's CPU path (the oracle port of QuSpin's OpenMP basis,
     CSR assembly and Taylor loop) on the host cores; each step a bounded
@@ -410,12 +495,17 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
+    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors"],
+                   help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
-    if args.L != 32:
+    if args.L != 32 and args.workload == "j1j2":
         WORKLOAD["L"] = args.L
         WORKLOAD["workload"] = "j1j2_chain_L{}_Sz0_k0_p+1_z+1_expm_t5".format(args.L)
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "sectors":
+        run_sectors(args)
+        return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")
         run_reference(args, rank, ws)

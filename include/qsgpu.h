@@ -132,6 +132,19 @@ int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, co
                      double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
                      void *d_work, int btype, void *d_ctl, int group, void *stream);
 
+/* ---- many sectors in one launch: block-diagonal stack of sector matrices,
+ * per-sector shift / factor / stopping test, common (s, m*) schedule.  The
+ * reference fans sectors out to processes (src/quspin/tools/block_tools.py:
+ * 135-220, 618-795); this replaces that fan-out for the expm path. ------ */
+int qs_multi_ctl_bytes(void);
+int qs_max_sectors(void);
+int qs_taylor_multi_term(int64_t n, const void *d_indptr, const int32_t *d_indices, const void *d_data, int dtype,
+                         const void *d_Bin, void *d_Bout, int btype, void *d_F, int64_t nvec, const int64_t *d_sec_off,
+                         const void *d_mu, const void *d_coeff, int j, double tol, void *d_ctl, int group,
+                         void *stream);
+int qs_taylor_multi_rescale(int64_t n, int64_t nvec, void *d_F, void *d_B0, int btype, const int64_t *d_sec_off,
+                            const void *d_eta, int use_eta, void *d_ctl, void *stream);
+
 /* ---- e^{aA} v without any device allocation.  No counterpart in the
  * reference: this entry point exists for callers that cannot allocate GPU
  * memory (a host application or plugin framework that owns the device memory

@@ -74,6 +74,11 @@ _SIGS = {
     "qs_expm_noalloc_max_elems": (_i64, []),
     "qs_expm_multiply_noalloc": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i64, _i, _i, _d, _d, _d, _d, _d,
                                       _i, _vp]),
+    "qs_multi_ctl_bytes": (_i, []),
+    "qs_max_sectors": (_i, []),
+    "qs_taylor_multi_term": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _vp, _vp, _vp, _i, _d, _vp, _i,
+                                  _vp]),
+    "qs_taylor_multi_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp]),
     "qs_lanczos_ctl_bytes": (_i, []),
     "qs_lanczos_scratch_doubles": (_i, []),
     "qs_lanczos_reorth_scratch_doubles": (_i64, [_i]),

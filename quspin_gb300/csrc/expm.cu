@@ -76,6 +76,17 @@ __device__ __forceinline__ void madd(cdbl &acc, cdbl d, cdbl x)
 
 __device__ __forceinline__ double cabs_(cdbl v) { return sqrt(v.x * v.x + v.y * v.y); }
 
+// F and the new term are touched once per term: stream them (evict-first)
+// so the gathered vector keeps its place in L2.
+__device__ __forceinline__ cdbl ldF(const cdbl *p)
+{
+    double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    return cdbl{v.x, v.y};
+}
+__device__ __forceinline__ void stF(cdbl *p, cdbl v) { __stcs(reinterpret_cast<double2 *>(p), make_double2(v.x, v.y)); }
+__device__ __forceinline__ void stB(cdbl *p, cdbl v) { __stcs(reinterpret_cast<double2 *>(p), make_double2(v.x, v.y)); }
+__device__ __forceinline__ void stB(cflt *p, cdbl v) { __stcs(reinterpret_cast<float2 *>(p), make_float2((float)v.x, (float)v.y)); }
+
 // block-wide max of two non-negative doubles, atomically folded into ctl
 __device__ __forceinline__ void fold_max2(double a, double b, unsigned long long *ga, unsigned long long *gb)
 {
@@ -154,20 +165,27 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
     for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
         const int64_t r = rb + gsub;
         const bool valid = r < n;
-        const int64_t k0 = valid ? (int64_t)indptr[r] : 0, k1 = valid ? (int64_t)indptr[r + 1] : 0;
+        const IT k0 = valid ? indptr[r] : (IT)0, k1 = valid ? indptr[r + 1] : (IT)0;
         double rb_ = 0.0, rf = 0.0;
+        // the row's own B and F entries do not depend on the gathers: load them
+        // first so their latency overlaps the row's gather loop
+        cdbl bo_pre{0.0, 0.0}, f_pre{0.0, 0.0};
+        if (NB == 1 && valid && lane == 0) {
+            bo_pre = BLoad<BT>::ld(Bin, r);
+            f_pre = ldF(F + r);
+        }
         for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
             cdbl acc[NB];
 #pragma unroll
             for (int b = 0; b < NB; b++) acc[b] = cdbl{0.0, 0.0};
-            for (int64_t k = k0 + lane; k < k1; k += G * U) {
-                int64_t col[U];
+            for (IT k = k0 + lane; k < k1; k += G * U) {
+                int32_t col[U];
                 DT d[U];
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int64_t kk = k + u * G;
+                    const IT kk = k + u * G;
                     const bool in = kk < k1;
-                    col[u] = in ? (int64_t)st_ld(indices + kk) : 0;
+                    col[u] = in ? st_ld(indices + kk) : 0;
                     d[u] = in ? st_ld(data + kk) : zro<DT>();
                 }
 #pragma unroll
@@ -175,7 +193,7 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
                     if (k + u * G < k1) {
 #pragma unroll
                         for (int b = 0; b < NB; b++)
-                            if (c0 + b < nvec) madd(acc[b], wid(d[u]), BLoad<BT>::ld(Bin, col[u] * nvec + c0 + b));
+                            if (c0 + b < nvec) madd(acc[b], wid(d[u]), BLoad<BT>::ld(Bin, (int64_t)col[u] * nvec + c0 + b));
                     }
                 }
             }
@@ -192,17 +210,24 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
                 for (int b = 0; b < NB; b++) {
                     if (c0 + b >= nvec) break;
                     const int64_t e = r * nvec + c0 + b;
-                    const cdbl bo = BLoad<BT>::ld(Bin, e);
+                    const cdbl bo = (NB == 1) ? bo_pre : BLoad<BT>::ld(Bin, e);
                     // w = A B - mu B
                     const double wr = acc[b].x - (mu.x * bo.x - mu.y * bo.y);
                     const double wi = acc[b].y - (mu.x * bo.y + mu.y * bo.x);
                     cdbl bn{cf.x * wr - cf.y * wi, cf.x * wi + cf.y * wr};
-                    BLoad<BT>::st(Bout, e, bn);
-                    cdbl f = F[e];
+                    stB(Bout + e, bn);
+                    cdbl f = (NB == 1) ? f_pre : ldF(F + e);
                     f.x += bn.x; f.y += bn.y;
-                    F[e] = f;
-                    rb_ += cabs_(bn);
-                    rf += cabs_(f);
+                    stF(F + e, f);
+                    if (NB == 1) {
+                        // one column: track squared moduli, take the square
+                        // root once (same value: sqrt is monotonic)
+                        rb_ = bn.x * bn.x + bn.y * bn.y;
+                        rf = f.x * f.x + f.y * f.y;
+                    } else {
+                        rb_ += cabs_(bn);
+                        rf += cabs_(f);
+                    }
                 }
             }
         }
@@ -214,6 +239,7 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
         volatile ExpmCtl *vc = ctl;
         double c2 = __longlong_as_double((long long)vc->c2);
         double fn = __longlong_as_double((long long)vc->fn);
+        if (nvec == 1) { c2 = sqrt(c2); fn = sqrt(fn); }
         vc->terms = vc->terms + 1;
         if (vc->c1 + c2 <= tol * fn) vc->done = 1;
         else vc->c1 = c2;
@@ -264,7 +290,7 @@ static int pick_group_e(int64_t n, int64_t nnz)
 {
     double avg = n > 0 ? (double)nnz / (double)n : 1.0;
     int g = 2;
-    while (g < 32 && g * 8 < avg) g <<= 1;
+    while (g < 32 && g * 24 < avg) g <<= 1;
     return g;
 }
 
@@ -405,5 +431,295 @@ extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int 
         rc = qs_taylor_rescale(n, nvec, F, b0, btype, eta, ctl, stream);
         if (rc) return rc;
     }
+    return QS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Many symmetry sectors in one launch.
+//
+// The sectors' CSR matrices are stacked block-diagonally (rows of sector b
+// are [sec_off[b], sec_off[b+1]), columns shifted the same way) and every
+// sector evolves its own block of k states with the common schedule
+// (s substeps, at most m* terms, coefficient a / (s (j+1))) but its own shift
+// mu_b, its own factor eta_b = exp(a mu_b / s) and its own stopping test on
+// the row sums of its block.  A sector whose test has fired is skipped by
+// the following launches of the substep.
+
+#define QS_MAX_SECTORS 64
+
+struct MultiCtl {
+    unsigned int arrive;
+    int nsec;
+    long long terms;                       // sector-terms executed
+    double c1[QS_MAX_SECTORS];
+    unsigned long long c2[QS_MAX_SECTORS];
+    unsigned long long fn[QS_MAX_SECTORS];
+    int done[QS_MAX_SECTORS];
+};
+
+extern "C" int qs_multi_ctl_bytes() { return (int)sizeof(MultiCtl); }
+extern "C" int qs_max_sectors() { return QS_MAX_SECTORS; }
+
+__device__ __forceinline__ int sector_of(const int64_t *soff, int nsec, int64_t r)
+{
+    int lo = 0, hi = nsec;          // largest b with soff[b] <= r
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (soff[mid] <= r) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ bool last_block_multi(MultiCtl *ctl)
+{
+    __shared__ bool is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int t = atomicAdd(&ctl->arrive, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return is_last;
+}
+
+template <typename DT, typename BT, typename IT, int G, int NB, int U>
+__global__ void __launch_bounds__(256) taylor_multi_kernel(int64_t n, const IT *__restrict__ indptr,
+                                                           const int32_t *__restrict__ indices,
+                                                           const DT *__restrict__ data, const BT *__restrict__ Bin,
+                                                           BT *__restrict__ Bout, cdbl *__restrict__ F, int64_t nvec,
+                                                           const int64_t *__restrict__ sec_off,
+                                                           const cdbl *__restrict__ mu, const cdbl *__restrict__ coeff,
+                                                           int j, double tol, MultiCtl *ctl)
+{
+    __shared__ int64_t soff[QS_MAX_SECTORS + 1];
+    __shared__ int sdone[QS_MAX_SECTORS];
+    __shared__ unsigned long long smb[QS_MAX_SECTORS], smf[QS_MAX_SECTORS];
+    const int nsec = ctl->nsec;
+    for (int b = threadIdx.x; b <= nsec; b += blockDim.x) soff[b] = sec_off[b];
+    for (int b = threadIdx.x; b < nsec; b += blockDim.x) {
+        sdone[b] = *((volatile int *)&ctl->done[b]);
+        smb[b] = 0ull;
+        smf[b] = 0ull;
+    }
+    __syncthreads();
+    const cdbl cf = coeff[j];
+    constexpr int GPW = 32 / G;
+    const int lane = threadIdx.x & (G - 1);
+    const int gsub = (threadIdx.x & 31) / G;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int64_t r = rb + gsub;
+        const int b = r < n ? sector_of(soff, nsec, r) : 0;
+        const bool valid = r < n && !sdone[b];
+        const IT k0 = valid ? indptr[r] : (IT)0, k1 = valid ? indptr[r + 1] : (IT)0;
+        double rb_ = 0.0, rf = 0.0;
+        for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
+            cdbl acc[NB];
+#pragma unroll
+            for (int q = 0; q < NB; q++) acc[q] = cdbl{0.0, 0.0};
+            for (IT k = k0 + lane; k < k1; k += G * U) {
+                int32_t col[U];
+                DT d[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const IT kk = k + u * G;
+                    const bool in = kk < k1;
+                    col[u] = in ? st_ld(indices + kk) : 0;
+                    d[u] = in ? st_ld(data + kk) : zro<DT>();
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    if (k + u * G < k1) {
+#pragma unroll
+                        for (int q = 0; q < NB; q++)
+                            if (c0 + q < nvec) madd(acc[q], wid(d[u]), BLoad<BT>::ld(Bin, (int64_t)col[u] * nvec + c0 + q));
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < NB; q++) {
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    acc[q].x += __shfl_down_sync(0xffffffffu, acc[q].x, o, G);
+                    acc[q].y += __shfl_down_sync(0xffffffffu, acc[q].y, o, G);
+                }
+            }
+            if (valid && lane == 0) {
+                const cdbl m = mu[b];
+#pragma unroll
+                for (int q = 0; q < NB; q++) {
+                    if (c0 + q >= nvec) break;
+                    const int64_t e = r * nvec + c0 + q;
+                    const cdbl bo = BLoad<BT>::ld(Bin, e);
+                    const double wr = acc[q].x - (m.x * bo.x - m.y * bo.y);
+                    const double wi = acc[q].y - (m.x * bo.y + m.y * bo.x);
+                    cdbl bn{cf.x * wr - cf.y * wi, cf.x * wi + cf.y * wr};
+                    BLoad<BT>::st(Bout, e, bn);
+                    cdbl f = F[e];
+                    f.x += bn.x; f.y += bn.y;
+                    F[e] = f;
+                    rb_ += cabs_(bn);
+                    rf += cabs_(f);
+                }
+            }
+        }
+        if (valid && lane == 0) {
+            atomicMax(&smb[b], (unsigned long long)__double_as_longlong(rb_));
+            atomicMax(&smf[b], (unsigned long long)__double_as_longlong(rf));
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nsec; b += blockDim.x) {
+        if (smb[b]) atomicMax(&ctl->c2[b], smb[b]);
+        if (smf[b]) atomicMax(&ctl->fn[b], smf[b]);
+    }
+    if (last_block_multi(ctl) && threadIdx.x == 0) {
+        volatile MultiCtl *vc = ctl;
+        long long active = 0;
+        for (int b = 0; b < nsec; b++) {
+            if (vc->done[b]) continue;
+            active++;
+            double c2 = __longlong_as_double((long long)vc->c2[b]);
+            double fn = __longlong_as_double((long long)vc->fn[b]);
+            if (vc->c1[b] + c2 <= tol * fn) vc->done[b] = 1;
+            else vc->c1[b] = c2;
+            vc->c2[b] = 0ull;
+            vc->fn[b] = 0ull;
+        }
+        vc->terms = vc->terms + active;
+        __threadfence();
+        vc->arrive = 0u;
+    }
+}
+
+// F = eta_b F; B0 = F; c1[b] = ||F_b||_inf; done[b] = 0.  use_eta = 0 for
+// the set-up before the first substep (eta = 1).
+template <typename BT>
+__global__ void __launch_bounds__(256) taylor_multi_rescale_kernel(int64_t n, int64_t nvec, cdbl *__restrict__ F,
+                                                                   BT *__restrict__ B0,
+                                                                   const int64_t *__restrict__ sec_off,
+                                                                   const cdbl *__restrict__ eta, int use_eta,
+                                                                   MultiCtl *ctl)
+{
+    __shared__ int64_t soff[QS_MAX_SECTORS + 1];
+    __shared__ unsigned long long sm[QS_MAX_SECTORS];
+    const int nsec = ctl->nsec;
+    for (int b = threadIdx.x; b <= nsec; b += blockDim.x) soff[b] = sec_off[b];
+    for (int b = threadIdx.x; b < nsec; b += blockDim.x) sm[b] = 0ull;
+    __syncthreads();
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int b = sector_of(soff, nsec, r);
+        const cdbl et = use_eta ? eta[b] : cdbl{1.0, 0.0};
+        double rs = 0.0;
+        for (int64_t c = 0; c < nvec; c++) {
+            const int64_t e = r * nvec + c;
+            cdbl f = F[e];
+            if (use_eta) {
+                cdbl g{et.x * f.x - et.y * f.y, et.x * f.y + et.y * f.x};
+                f = g;
+                F[e] = f;
+            }
+            BLoad<BT>::st(B0, e, f);
+            rs += cabs_(f);
+        }
+        atomicMax(&sm[b], (unsigned long long)__double_as_longlong(rs));
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nsec; b += blockDim.x)
+        if (sm[b]) atomicMax(&ctl->c2[b], sm[b]);
+    if (last_block_multi(ctl) && threadIdx.x == 0) {
+        volatile MultiCtl *vc = ctl;
+        for (int b = 0; b < nsec; b++) {
+            vc->c1[b] = __longlong_as_double((long long)vc->c2[b]);
+            vc->c2[b] = 0ull;
+            vc->fn[b] = 0ull;
+            vc->done[b] = 0;
+        }
+        __threadfence();
+        vc->arrive = 0u;
+    }
+}
+
+template <typename DT, typename BT, int NB, int U>
+static int multi_launch(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *Bin,
+                        void *Bout, cdbl *F, int64_t nvec, const int64_t *soff, const cdbl *mu, const cdbl *coeff, int j,
+                        double tol, MultiCtl *ctl, int G, cudaStream_t st)
+{
+    int blocks = grid_for(n, G);
+#define L_(GG) taylor_multi_kernel<DT, BT, int32_t, GG, NB, U><<<blocks, 256, 0, st>>>(n, (const int32_t *)indptr, indices, (const DT *)data, (const BT *)Bin, (BT *)Bout, F, nvec, soff, mu, coeff, j, tol, ctl)
+    switch (G) {
+    case 2: L_(2); break;
+    case 4: L_(4); break;
+    case 8: L_(8); break;
+    case 16: L_(16); break;
+    default: L_(32); break;
+    }
+#undef L_
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+template <typename DT, typename BT>
+static int multi_nb(int64_t n, const void *indptr, const int32_t *indices, const void *data, const void *Bin,
+                    void *Bout, cdbl *F, int64_t nvec, const int64_t *soff, const cdbl *mu, const cdbl *coeff, int j,
+                    double tol, MultiCtl *ctl, int G, int U, cudaStream_t st)
+{
+    if (nvec == 1) {
+        if (U >= 2) return multi_launch<DT, BT, 1, 2>(n, indptr, indices, data, Bin, Bout, F, nvec, soff, mu, coeff, j, tol, ctl, G, st);
+        return multi_launch<DT, BT, 1, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, soff, mu, coeff, j, tol, ctl, G, st);
+    }
+    if (nvec == 2) return multi_launch<DT, BT, 2, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, soff, mu, coeff, j, tol, ctl, G, st);
+    if (nvec <= 4) return multi_launch<DT, BT, 4, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, soff, mu, coeff, j, tol, ctl, G, st);
+    return multi_launch<DT, BT, 8, 1>(n, indptr, indices, data, Bin, Bout, F, nvec, soff, mu, coeff, j, tol, ctl, G, st);
+}
+
+// One Taylor term for every sector of a block-diagonal stack (int32 indptr).
+// sec_off: device int64[nsec+1] row offsets; mu: device complex128[nsec];
+// coeff: device complex128 table; ctl: MultiCtl (qs_multi_ctl_bytes()) with
+// nsec set.  dtype QS_F64 / QS_C128 with btype QS_C128, or QS_F32 / QS_C64 /
+// QS_F64 with btype QS_C64.  group as for qs_taylor_term.
+extern "C" int qs_taylor_multi_term(int64_t n, const void *indptr, const int32_t *indices, const void *data, int dtype,
+                                    const void *Bin, void *Bout, int btype, void *F, int64_t nvec,
+                                    const int64_t *sec_off, const void *mu, const void *coeff, int j, double tol,
+                                    void *ctl, int group, void *stream)
+{
+    if (n < 1 || nvec < 1 || !indptr || !Bin || !Bout || !F || !sec_off || !mu || !coeff || !ctl || j < 0)
+        return QS_ERR_ARG;
+    int G = group > 0 ? (group & 0xff) : 4;
+    int U = group > 0 ? ((group >> 8) & 0xff) : 2;
+    if (G != 2 && G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
+    cudaStream_t st = qs_stream(stream);
+    MultiCtl *c = reinterpret_cast<MultiCtl *>(ctl);
+    const cdbl *m = reinterpret_cast<const cdbl *>(mu);
+    const cdbl *cf = reinterpret_cast<const cdbl *>(coeff);
+    cdbl *Fp = reinterpret_cast<cdbl *>(F);
+    if (btype == QS_C128) {
+        if (dtype == QS_F64) return multi_nb<double, cdbl>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
+        if (dtype == QS_C128) return multi_nb<cdbl, cdbl>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
+    } else if (btype == QS_C64) {
+        if (dtype == QS_F32) return multi_nb<float, cflt>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
+        if (dtype == QS_C64) return multi_nb<cflt, cflt>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
+        if (dtype == QS_F64) return multi_nb<double, cflt>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
+    }
+    return QS_ERR_ARG;
+}
+
+extern "C" int qs_taylor_multi_rescale(int64_t n, int64_t nvec, void *F, void *B0, int btype, const int64_t *sec_off,
+                                       const void *eta, int use_eta, void *ctl, void *stream)
+{
+    if (n < 1 || nvec < 1 || !F || !B0 || !sec_off || !ctl || (use_eta && !eta)) return QS_ERR_ARG;
+    cudaStream_t st = qs_stream(stream);
+    int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
+    int blocks = (int)(b > cap ? cap : b);
+    if (btype == QS_C128)
+        taylor_multi_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, sec_off,
+                                                                 (const cdbl *)eta, use_eta, (MultiCtl *)ctl);
+    else if (btype == QS_C64)
+        taylor_multi_rescale_kernel<cflt><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cflt *)B0, sec_off,
+                                                                 (const cdbl *)eta, use_eta, (MultiCtl *)ctl);
+    else return QS_ERR_ARG;
+    QS_CHECK(cudaGetLastError());
     return QS_OK;
 }

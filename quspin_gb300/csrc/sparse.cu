@@ -126,19 +126,19 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
     for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
         const int64_t r = rb + gsub;
         const bool valid = r < n;
-        const int64_t k0 = valid ? (int64_t)indptr[r] : 0, k1 = valid ? (int64_t)indptr[r + 1] : 0;
+        const IT k0 = valid ? indptr[r] : (IT)0, k1 = valid ? indptr[r + 1] : (IT)0;
         for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
             ACC acc[NB];
 #pragma unroll
             for (int b = 0; b < NB; b++) set_zero(acc[b]);
-            for (int64_t k = k0 + lane; k < k1; k += G * U) {
-                int64_t col[U];
+            for (IT k = k0 + lane; k < k1; k += G * U) {
+                int32_t col[U];
                 DT d[U];
 #pragma unroll
                 for (int u = 0; u < U; u++) {
-                    const int64_t kk = k + u * G;
+                    const IT kk = k + u * G;
                     const bool in = kk < k1;
-                    col[u] = in ? (int64_t)ld_stream(indices + kk) : 0;
+                    col[u] = in ? ld_stream(indices + kk) : 0;
                     d[u] = in ? ld_stream(data + kk) : zero_of<DT>();
                 }
 #pragma unroll
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
                     if (k + u * G < k1) {
 #pragma unroll
                         for (int b = 0; b < NB; b++)
-                            if (c0 + b < nvec) fma_acc(acc[b], widen(d[u]), Num<XT>::ld(x, col[u] * nvec + c0 + b));
+                            if (c0 + b < nvec) fma_acc(acc[b], widen(d[u]), Num<XT>::ld(x, (int64_t)col[u] * nvec + c0 + b));
                     }
                 }
             }
@@ -164,12 +164,13 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int64_t n, const IT *__re
     }
 }
 
-// Lanes per row from the mean row length: about eight entries per lane.
+// Lanes per row from the mean row length: about 12-24 entries per lane (random
+// gathers favour few lanes per row; the tuner refines this).
 static int pick_group(int64_t n, int64_t nnz)
 {
     double avg = n > 0 ? (double)nnz / (double)n : 1.0;
     int g = 2;
-    while (g < 32 && g * 8 < avg) g <<= 1;
+    while (g < 32 && g * 24 < avg) g <<= 1;
     return g;
 }
 

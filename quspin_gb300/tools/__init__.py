@@ -1,7 +1,8 @@
 """GPU tools of the hot path: expm_multiply_parallel, Lanczos, matvec."""
+from .batched import MultiSectorExpm
 from .expm_multiply_parallel import ExpmMultiplyParallel, expm_multiply_parallel
 from .lanczos import expm_lanczos, lanczos_full, lanczos_iter, lin_comb_Q_T
 from .matvec import get_matvec_function, matvec
 
 __all__ = ["ExpmMultiplyParallel", "expm_multiply_parallel", "lanczos_full", "lanczos_iter", "lin_comb_Q_T",
-           "expm_lanczos", "matvec", "get_matvec_function"]
+           "expm_lanczos", "matvec", "get_matvec_function", "MultiSectorExpm"]

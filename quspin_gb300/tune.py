@@ -23,11 +23,11 @@ def encode(G, U):
 
 
 def _candidates(n, nnz, nvec):
+    """Shapes to time: 2, 4, 8 lanes per row (16 / 32 for long rows) x 1, 2, 4
+    entries in flight (one column) -- gathers of random columns favour few
+    lanes per row."""
     avg = nnz / max(n, 1)
-    g = 2
-    while g < 32 and g * 8 < avg:
-        g <<= 1
-    Gs = sorted({max(2, g // 2), g, min(32, g * 2)})
+    Gs = [2, 4, 8] + ([16] if avg >= 32 else []) + ([32] if avg >= 64 else [])
     Us = (1, 2, 4) if nvec == 1 else (1,)
     return [(G, U) for G in Gs for U in Us]
 
