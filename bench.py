@@ -409,7 +409,7 @@ def run_sectors(args):
     ref = [o.clone() for o in outs]
     res = {}
     for prec in ("double", "mixed"):
-        ms = MultiSectorExpm(mats, a=-1j * T, nvec=k, precision=prec)
+        ms = MultiSectorExpm(plain, a=-1j * T, nvec=k, precision=prec)
         for _ in range(args.warmup):
             ms.load(blocks)
             ms.run_device()
@@ -433,6 +433,91 @@ def run_sectors(args):
            "dims": [M.shape[0] for M in mats], "build_s": round(t_build, 3),
            "plain_fp64_per_block_loop": {"evolutions_per_s": len(mats) * k / t_plain, "s_per_step": t_plain},
            "stacked_fp64": res["double"], "stacked_mixed": res["mixed"]}
+    print(json.dumps(out))
+
+
+def run_driven(args):
+    """Learned-partition workload: driven Ising chain L=26 (k=0, p=+1),
+    H(t) = -sum zz - (h0 + A cos wt) sum x - 0.2 sum z, h0=0.8, A=0.5,
+    w=2 pi; 32 seeded states; 200 piecewise-constant steps per period.
+    Plain per-step selection (exact 1-norm + fragment 3.1) vs the learned
+    predictor (trained here on the plain method's labels for (h0, A, w) drawn
+    within +-30%), both on the batched FP64 path; plus the plain selection
+    applied one state at a time (the unbatched FP64 path)."""
+    import torch
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    from quspin_gb300.learned import PartitionPredictor
+    from quspin_gb300.tools.driven import DrivenEvolution
+    L = args.L if args.L != 32 else 26
+    periods = args.periods
+    s_ = np.arange(L)
+    b = spin_basis_general(L, kblock=((s_ + 1) % L, 0), pblock=(s_[::-1].copy(), 0))
+    static = [["zz", [[-1.0, i, (i + 1) % L] for i in range(L)]], ["z", [[-0.2, i] for i in range(L)]]]
+    drive = lambda t, h0, A, w: h0 + A * np.cos(w * t)
+
+    def ham(h0, A, w):
+        dyn = [["x", [[-1.0, i] for i in range(L)], drive, (h0, A, w)]]
+        return hamiltonian(static, dyn, basis=b, dtype=np.float64)
+    h0, A, w = 0.8, 0.5, 2 * np.pi
+    T = 2 * np.pi / w
+    dt = T / 200
+    nsteps = 200 * periods
+    k = 32
+    # training data from the plain selection over the +-30% box
+    rng = np.random.default_rng(0)
+    t0 = time.perf_counter()
+    feats, ms, ss = [], [], []
+    for _ in range(6):
+        hh, AA, ww = (h0 * rng.uniform(0.7, 1.3), A * rng.uniform(0.7, 1.3), w * rng.uniform(0.7, 1.3))
+        evt = DrivenEvolution(ham(hh, AA, ww), nvec=1)
+        tt = rng.uniform(0, 2 * np.pi / ww, 60)
+        dd = (2 * np.pi / ww / 200) * 10 ** rng.uniform(-0.3, 1.3, 60)
+        f, m_, s2 = evt.training_set(tt, dd)
+        feats.append(f); ms.append(m_); ss.append(s2)
+    feats, ms, ss = np.concatenate(feats), np.concatenate(ms), np.concatenate(ss)
+    t_data = time.perf_counter() - t0
+    pred = PartitionPredictor(n_coeffs=1, seed=0)
+    t0 = time.perf_counter()
+    hist = pred.fit(feats, ms, ss, epochs=200, lr=3e-3, batch=128)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    H = ham(h0, A, w)
+    ev = DrivenEvolution(H, nvec=k)
+    V = rng.normal(size=(H.Ns, k)) + 1j * rng.normal(size=(H.Ns, k))
+    V /= np.linalg.norm(V, axis=0)
+    V0 = torch.tensor(V, device="cuda")
+    res = {}
+    for mode in ("plain", "learned"):
+        F = V0.clone()
+        ev.fallbacks = 0
+        ev.norm_passes = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev.run(F, 0.0, dt, nsteps, mode=mode, predictor=pred, segment=100)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        res[mode] = {"seconds": el, "state_evolutions_per_s": k * nsteps / el, "norm_passes": ev.norm_passes,
+                     "fallback_segments": ev.fallbacks, "F": F}
+    err = float(torch.linalg.vector_norm(res["learned"]["F"] - res["plain"]["F"]) /
+                torch.linalg.vector_norm(res["plain"]["F"]))
+    # unbatched plain: one state at a time, a few steps, scaled
+    ev1 = DrivenEvolution(H, nvec=1)
+    F1 = V0[:, :1].clone().contiguous()
+    n1 = min(nsteps, 100)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev1.run(F1, 0.0, dt, n1, mode="plain")
+    torch.cuda.synchronize()
+    el1 = time.perf_counter() - t0
+    out = {"metric": "expm_multiply evolutions/s", "workload": "driven_ising_L{}_k0_p0_32_states_{}_periods".format(
+        L, periods), "unit": "state-steps/s (one state through one piecewise step)",
+        "Ns": H.Ns, "steps": nsteps, "dt": dt,
+        "plain_batched": {x: y for x, y in res["plain"].items() if x != "F"},
+        "learned_batched": {x: y for x, y in res["learned"].items() if x != "F"},
+        "plain_unbatched": {"state_evolutions_per_s": n1 / el1, "sample_steps": n1},
+        "learned_vs_plain_rel_state_error": err,
+        "training": {"samples": int(len(ms)), "label_seconds": t_data, "train_seconds": t_train,
+                     "final_loss": hist[-1], "first_loss": hist[0]}}
     print(json.dumps(out))
 
 
@@ -495,7 +580,8 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
-    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors"],
+    p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
+    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven"],
                    help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
     if args.L != 32 and args.workload == "j1j2":
@@ -505,6 +591,9 @@ def main():
         args.warmup = 3
     if args.workload == "sectors":
         run_sectors(args)
+        return
+    if args.workload == "driven":
+        run_driven(args)
         return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")

@@ -90,6 +90,14 @@ int qs_csr_compact(int vtype, int64_t Ns, const int64_t *d_rowptr, const uint64_
                    const int64_t *d_incl, void *d_indptr, int idx64, int32_t *d_indices, void *d_data,
                    void *stream);
 
+/* ---- conjugate transpose A^H on the device: the rmatvec operand of the
+ * onenormest products in ExpmMultiplyParallel's norm information
+ * (html expm_multiply_parallel_core.html:436-449).  count -> scan -> fill ->
+ * qs_csr_merge (no diagonal) -> scan -> qs_csr_compact. --------------------- */
+int qs_csr_t_count(int64_t n, const void *d_indptr, int idx64, const int32_t *d_indices, int64_t *d_cnt, void *stream);
+int qs_csr_t_fill(int vtype, int64_t n, const void *d_indptr, int idx64, const int32_t *d_indices, const void *d_data,
+                  const int64_t *d_rowptr, int64_t *d_cursor, uint64_t *d_keys, void *d_vals, void *stream);
+
 /* ---- _core.inplace_op (base_general.py:395-408): matrix-free apply ------ */
 int qs_inplace_op(void *sym, const void *d_states, const uint32_t *d_norms, int64_t Ns, int N_p,
                   const int64_t *d_begin, const int64_t *d_end, const int32_t *t_nop, const int32_t *t_off,
@@ -126,7 +134,7 @@ int qs_taylor_term(int64_t n, int64_t nnz, const void *d_indptr, int idx64, cons
                    int64_t nvec, double mu_re, double mu_im, const void *d_coeff, int j, double tol, void *d_ctl,
                    int group, void *stream);
 int qs_taylor_rescale(int64_t n, int64_t nvec, void *d_F, void *d_B0, int btype, const void *d_eta, void *d_ctl,
-                      void *stream);
+                      int substep_end, void *stream);
 int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                      const void *d_data, int dtype, void *d_F, int64_t nvec, int s, int m_star, double tol,
                      double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
@@ -144,6 +152,21 @@ int qs_taylor_multi_term(int64_t n, const void *d_indptr, const int32_t *d_indic
                          void *stream);
 int qs_taylor_multi_rescale(int64_t n, int64_t nvec, void *d_F, void *d_B0, int btype, const int64_t *d_sec_off,
                             const void *d_eta, int use_eta, void *d_ctl, void *stream);
+
+/* ---- dense layers of the learned (m*, s) predictor (no counterpart in
+ * the reference, whose selection is scipy's onenormest-based fragment 3.1,
+ * html expm_multiply_parallel_core.html:377-463): y = act(x W^T + b) with
+ * bfloat16 weights and FP32 accumulation, the matching backward products, a
+ * weighted mean-squared-error gradient and an Adam update. ----------------- */
+int qs_mlp_dense_fwd(int B, int din, int dout, const float *d_x, const void *d_w_bf16, const float *d_bias,
+                     float *d_z, float *d_y, int relu, void *stream);
+int qs_mlp_dense_bwd(int B, int din, int dout, const float *d_dy, const void *d_w_bf16, const float *d_x,
+                     const float *d_zin, float *d_dx, float *d_gw, float *d_gb, void *stream);
+int qs_mlp_mse(int64_t total, int dout, const float *d_y, const float *d_target, const float *d_colw, float scale,
+               float *d_dy, float *d_partial, int nblocks, void *stream);
+int qs_mlp_adam(int64_t n, float *d_w, const float *d_g, float *d_m, float *d_v, void *d_w_bf16, float lr, float b1,
+                float b2, float eps, int step, void *stream);
+int qs_mlp_to_bf16(int64_t n, const float *d_w, void *d_w_bf16, void *stream);
 
 /* ---- e^{aA} v without any device allocation.  No counterpart in the
  * reference: this entry point exists for callers that cannot allocate GPU

@@ -56,6 +56,8 @@ _SIGS = {
     "qs_csr_diag": (_i, [_vp, _i, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     "qs_csr_merge": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qs_csr_compact": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
+    "qs_csr_t_count": (_i, [_i64, _vp, _i, _vp, _vp, _vp]),
+    "qs_csr_t_fill": (_i, [_i, _i64, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qs_inplace_op": (_i, [_vp, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _vp,
                            _vp, _i64, _vp, _vp]),
     "qs_csr_matvec": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp]),
@@ -68,7 +70,7 @@ _SIGS = {
     "qs_expm_ctl_bytes": (_i, []),
     "qs_taylor_term": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _d, _d, _vp, _i, _d, _vp,
                             _i, _vp]),
-    "qs_taylor_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _vp]),
+    "qs_taylor_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp]),
     "qs_expm_multiply": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i64, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp,
                               _i, _vp, _i, _vp]),
     "qs_expm_noalloc_max_elems": (_i64, []),
@@ -79,6 +81,12 @@ _SIGS = {
     "qs_taylor_multi_term": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _vp, _vp, _vp, _i, _d, _vp, _i,
                                   _vp]),
     "qs_taylor_multi_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp]),
+    "qs_mlp_dense_fwd": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+    "qs_mlp_dense_bwd": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qs_mlp_mse": (_i, [_i64, _i, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _i, _vp]),
+    "qs_mlp_adam": (_i, [_i64, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                         ctypes.c_float, _i, _vp]),
+    "qs_mlp_to_bf16": (_i, [_i64, _vp, _vp, _vp]),
     "qs_lanczos_ctl_bytes": (_i, []),
     "qs_lanczos_scratch_doubles": (_i, []),
     "qs_lanczos_reorth_scratch_doubles": (_i64, [_i]),

@@ -1374,3 +1374,79 @@ extern "C" int qs_inplace_op(void *sym, const void *states, const uint32_t *norm
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// conjugate transpose of a CSR matrix (the rmatvec operand of the 1-norm
+// estimator): entries are bucketed by column, then the row merge above puts
+// each new row in ascending order.  Keys carry the original row in the
+// column position of the merge's (column, term) key.
+
+template <typename IT>
+__global__ void csr_t_count_kernel(int64_t n, const IT *__restrict__ indptr, const int32_t *__restrict__ indices,
+                                   int64_t *__restrict__ cnt)
+{
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        for (IT k = indptr[r]; k < indptr[r + 1]; k++) atomicAdd((unsigned long long *)&cnt[indices[k]], 1ull);
+}
+
+template <typename T> __device__ __forceinline__ T conj_of(T v) { return v; }
+template <> __device__ __forceinline__ cdbl conj_of<cdbl>(cdbl v) { return cdbl{v.x, -v.y}; }
+template <> __device__ __forceinline__ cflt conj_of<cflt>(cflt v) { return cflt{v.x, -v.y}; }
+
+template <typename T, typename IT>
+__global__ void csr_t_fill_kernel(int64_t n, const IT *__restrict__ indptr, const int32_t *__restrict__ indices,
+                                  const T *__restrict__ data, const int64_t *__restrict__ rowptr,
+                                  int64_t *__restrict__ cursor, uint64_t *__restrict__ keys, T *__restrict__ vals)
+{
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        for (IT k = indptr[r]; k < indptr[r + 1]; k++) {
+            const int64_t c = indices[k];
+            const int64_t slot = rowptr[c] + (int64_t)atomicAdd((unsigned long long *)&cursor[c], 1ull);
+            keys[slot] = (uint64_t)r << (TERM_BITS + POS_BITS);
+            vals[slot] = conj_of(data[k]);
+        }
+}
+
+template <typename T>
+static int csr_t_fill_t(int64_t n, const void *indptr, int idx64, const int32_t *indices, const void *data,
+                        const int64_t *rowptr, int64_t *cursor, uint64_t *keys, void *vals, cudaStream_t st)
+{
+    int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 16;
+    unsigned blocks = (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+    if (idx64)
+        csr_t_fill_kernel<T, int64_t><<<blocks, 256, 0, st>>>(n, (const int64_t *)indptr, indices, (const T *)data,
+                                                               rowptr, cursor, keys, (T *)vals);
+    else
+        csr_t_fill_kernel<T, int32_t><<<blocks, 256, 0, st>>>(n, (const int32_t *)indptr, indices, (const T *)data,
+                                                               rowptr, cursor, keys, (T *)vals);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+// Column counts of an n x n CSR into cnt[1 + col] (cnt zeroed, int64[n+1]).
+extern "C" int qs_csr_t_count(int64_t n, const void *indptr, int idx64, const int32_t *indices, int64_t *cnt,
+                              void *stream)
+{
+    if (n < 0 || !indptr || !cnt) return QS_ERR_ARG;
+    if (n == 0) return QS_OK;
+    cudaStream_t st = qs_stream(stream);
+    int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 16;
+    unsigned blocks = (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+    if (idx64) csr_t_count_kernel<int64_t><<<blocks, 256, 0, st>>>(n, (const int64_t *)indptr, indices, cnt + 1);
+    else csr_t_count_kernel<int32_t><<<blocks, 256, 0, st>>>(n, (const int32_t *)indptr, indices, cnt + 1);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+// Scatter the conjugated entries into column buckets (rowptr: inclusive scan
+// of the counts; cursor zeroed); then qs_csr_merge (no diagonal array) and
+// qs_csr_compact produce the canonical conjugate transpose.
+extern "C" int qs_csr_t_fill(int vtype, int64_t n, const void *indptr, int idx64, const int32_t *indices,
+                             const void *data, const int64_t *rowptr, int64_t *cursor, uint64_t *keys, void *vals,
+                             void *stream)
+{
+    if (n < 0 || !indptr || !rowptr || !cursor) return QS_ERR_ARG;
+    if (n == 0) return QS_OK;
+    if (n >= ((int64_t)1 << (64 - TERM_BITS - POS_BITS))) return QS_ERR_UNSUPPORTED;
+    DISPATCH_VT(vtype, csr_t_fill_t, n, indptr, idx64, indices, data, rowptr, cursor, keys, vals, qs_stream(stream));
+}

@@ -32,6 +32,8 @@ struct ExpmCtl {
     int done;                  // stopping test fired in this substep
     unsigned int arrive;       // blocks finished in the current launch
     long long terms;           // Taylor terms executed so far
+    int nonconv;               // substeps that used all m* terms without the test firing
+    int pad;
 };
 
 extern "C" int qs_expm_ctl_bytes() { return (int)sizeof(ExpmCtl); }
@@ -250,11 +252,13 @@ __global__ void __launch_bounds__(256) taylor_term_kernel(int64_t n, const IT *_
     }
 }
 
-// F = eta F; B0 = F; ctl->c1 = ||F||_inf; ctl->done = 0.
+// F = eta F; B0 = F; ctl->c1 = ||F||_inf; ctl->done = 0.  At the end of a
+// substep (substep_end) a stopping test that never fired is counted in
+// ctl->nonconv.
 template <typename BT>
 __global__ void __launch_bounds__(256) taylor_rescale_kernel(int64_t n, int64_t nvec, cdbl *__restrict__ F,
                                                              BT *__restrict__ B0, const cdbl *__restrict__ eta_p,
-                                                             ExpmCtl *ctl)
+                                                             ExpmCtl *ctl, int substep_end)
 {
     const cdbl eta = *eta_p;
     const bool scale = !(eta.x == 1.0 && eta.y == 0.0);
@@ -280,6 +284,7 @@ __global__ void __launch_bounds__(256) taylor_rescale_kernel(int64_t n, int64_t 
         vc->c1 = __longlong_as_double((long long)vc->c2);
         vc->c2 = 0ull;
         vc->fn = 0ull;
+        if (substep_end && !vc->done) vc->nonconv = vc->nonconv + 1;
         vc->done = 0;
         __threadfence();
         vc->arrive = 0u;
@@ -385,9 +390,11 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
 }
 
 // F = eta F; B0 = F; c1 = ||F||_inf; done = 0 (eta: device complex128).
-// With eta = 1 this is the set-up before the first substep.
+// With eta = 1 and substep_end = 0 this is the set-up before the first
+// substep; with substep_end = 1 a substep whose stopping test never fired is
+// counted in the control block.
 extern "C" int qs_taylor_rescale(int64_t n, int64_t nvec, void *F, void *B0, int btype, const void *eta, void *ctl,
-                                 void *stream)
+                                 int substep_end, void *stream)
 {
     if (n < 1 || nvec < 1 || !F || !B0 || !eta || !ctl) return QS_ERR_ARG;
     cudaStream_t st = qs_stream(stream);
@@ -395,10 +402,10 @@ extern "C" int qs_taylor_rescale(int64_t n, int64_t nvec, void *F, void *B0, int
     int blocks = (int)(b > cap ? cap : b);
     if (btype == QS_C128)
         taylor_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, (const cdbl *)eta,
-                                                           (ExpmCtl *)ctl);
+                                                           (ExpmCtl *)ctl, substep_end);
     else if (btype == QS_C64)
         taylor_rescale_kernel<cflt><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cflt *)B0, (const cdbl *)eta,
-                                                           (ExpmCtl *)ctl);
+                                                           (ExpmCtl *)ctl, substep_end);
     else return QS_ERR_ARG;
     QS_CHECK(cudaGetLastError());
     return QS_OK;
@@ -418,7 +425,7 @@ extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int 
     size_t esz = btype == QS_C128 ? 16 : 8;
     char *b0 = reinterpret_cast<char *>(work);
     char *b1 = b0 + (size_t)n * nvec * esz;
-    int rc = qs_taylor_rescale(n, nvec, F, b0, btype, one, ctl, stream);
+    int rc = qs_taylor_rescale(n, nvec, F, b0, btype, one, ctl, 0, stream);
     if (rc) return rc;
     for (int i = 0; i < s; i++) {
         for (int j = 0; j < m_star; j++) {
@@ -428,7 +435,7 @@ extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int 
                                 coeff, j, tol, ctl, group, stream);
             if (rc) return rc;
         }
-        rc = qs_taylor_rescale(n, nvec, F, b0, btype, eta, ctl, stream);
+        rc = qs_taylor_rescale(n, nvec, F, b0, btype, eta, ctl, m_star > 0 ? 1 : 0, stream);
         if (rc) return rc;
     }
     return QS_OK;

@@ -85,6 +85,39 @@ class DeviceCSR:
     def dot(self, V, out=None, a=1.0, overwrite_out=True):
         return _apply(self, V, out, a, overwrite_out)
 
+    def conj_transpose(self):
+        """A^H as a canonical device CSR (built on the device)."""
+        n = self.shape[0]
+        if self.shape[0] != self.shape[1]:
+            raise ValueError("square matrices only")
+        L = _lib.load()
+        st = D.stream()
+        vt = D.code(self.dtype)
+        cnt = torch.zeros(n + 1, dtype=torch.int64, device=D.device())
+        _lib.call("qs_csr_t_count", n, D.ptr(self.indptr), self.idx64, D.ptr(self.indices), D.ptr(cnt), st)
+        scr = torch.empty(max(L.qs_scan_scratch_elems(n), 1), dtype=torch.int64, device=D.device())
+        _lib.call("qs_scan_inclusive_i64", D.ptr(cnt[1:]), n, D.ptr(scr), st)
+        nnz = self.nnz
+        keys = torch.empty(max(nnz, 1), dtype=torch.int64, device=D.device())
+        vals = torch.empty(max(nnz, 1), dtype=D.torch_dtype(self.dtype), device=D.device())
+        cursor = torch.zeros(n, dtype=torch.int64, device=D.device())
+        _lib.call("qs_csr_t_fill", vt, n, D.ptr(self.indptr), self.idx64, D.ptr(self.indices), D.ptr(self.data),
+                  D.ptr(cnt), D.ptr(cursor), D.ptr(keys), D.ptr(vals), st)
+        mcount = torch.empty(n, dtype=torch.int64, device=D.device())
+        err = D.err_flag()
+        _lib.call("qs_csr_merge", vt, n, D.ptr(cnt), D.ptr(cursor), D.ptr(keys), D.ptr(vals), None, D.ptr(mcount),
+                  D.ptr(err), st)
+        if int(err.item()) & 8:
+            return DeviceCSR.from_scipy(self.tocsr().conj().T.tocsr(), self.dtype)
+        _lib.call("qs_scan_inclusive_i64", D.ptr(mcount), n, D.ptr(scr), st)
+        nnz2 = int(mcount[-1].item()) if n else 0
+        indptr = torch.empty(n + 1, dtype=self.indptr.dtype, device=D.device())
+        indices = torch.empty(max(nnz2, 1), dtype=torch.int32, device=D.device())
+        data = torch.empty(max(nnz2, 1), dtype=D.torch_dtype(self.dtype), device=D.device())
+        _lib.call("qs_csr_compact", vt, n, D.ptr(cnt), D.ptr(keys), D.ptr(vals), D.ptr(mcount), D.ptr(indptr),
+                  self.idx64, D.ptr(indices), D.ptr(data), st)
+        return DeviceCSR(indptr, indices[:nnz2], data[:nnz2], self.shape, self.dtype)
+
     def trace(self):
         if self.dtype not in (np.dtype(np.float64), np.dtype(np.complex128)):
             return self.astype(result_dtype(self.dtype, np.float64)).trace()

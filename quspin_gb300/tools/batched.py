@@ -58,13 +58,16 @@ class MultiSectorExpm:
     def __init__(self, matrices, a, nvec=1, precision="double", graph=True):
         if precision not in ("double", "mixed"):
             raise ValueError("precision must be 'double' or 'mixed'")
-        mats = [_as_device_csr(M) for M in matrices]
-        if len(mats) > _lib.load().qs_max_sectors():
+        if len(matrices) > _lib.load().qs_max_sectors():
             raise ValueError("at most {} sectors per launch".format(_lib.load().qs_max_sectors()))
         self._a = complex(a)
         self.nvec = int(nvec)
         self.precision = precision
-        self._plain = [ExpmMultiplyParallel(M, a=a) for M in mats]
+        # an ExpmMultiplyParallel with the same a can be passed instead of a
+        # matrix: its shift and (m*, s) are reused
+        self._plain = [M if isinstance(M, ExpmMultiplyParallel) and complex(M.a) == self._a
+                       else ExpmMultiplyParallel(M, a=a) for M in matrices]
+        mats = [p.A_device for p in self._plain]
         self.sizes = [M.shape[0] for M in mats]
         self.m_star = max(p.m_star for p in self._plain)
         self.s = max(p.s for p in self._plain)

@@ -126,7 +126,7 @@ class ExpmMultiplyParallel:
         if conj:
             a, mu = np.conj(a), np.conj(mu)
             if self._AH is None:
-                self._AH = DeviceCSR.from_scipy(self._Ad.tocsr().conj().T.tocsr(), self._Ad.dtype)
+                self._AH = self._Ad.conj_transpose()
             M = self._AH
         else:
             M = self._Ad
@@ -200,6 +200,13 @@ class ExpmMultiplyParallel:
         self._last_ctl = ctl
         self._consts = consts     # keep alive until the stream reaches it
         return F
+
+    @property
+    def nonconverged_substeps(self):
+        """Substeps of the last dot that used all m* terms without the
+        stopping test firing (reads the device counter)."""
+        c = getattr(self, "_last_ctl", None)
+        return 0 if c is None else int(c[5].view(torch.int32)[0].item())
 
     @property
     def terms_executed(self):

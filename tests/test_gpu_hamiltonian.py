@@ -139,3 +139,18 @@ def test_dot_out_semantics(cuda):
     np.testing.assert_allclose(yd.cpu().numpy(), Hs @ v, rtol=0, atol=1e-12)
     with pytest.raises(ValueError):
         H.dot(np.zeros(b.Ns + 1))
+
+
+def test_conj_transpose(cuda):
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    m = chain_maps(10)
+    b = spin_basis_general(10, kblock=(m["t"], 3))
+    st = [["xy", [[0.3, i, (i + 1) % 10] for i in range(10)]], ["zz", [[0.7, i, (i + 2) % 10] for i in range(10)]],
+          ["x", [[0.2, i] for i in range(10)]]]
+    A = hamiltonian(st, [], basis=b, dtype=np.complex128).tocsr_gpu()
+    AH = A.conj_transpose().tocsr()
+    ref = sp.csr_matrix(A.tocsr().conj().T)
+    ref.sort_indices()
+    np.testing.assert_array_equal(AH.indptr, ref.indptr)
+    np.testing.assert_array_equal(AH.indices, ref.indices)
+    np.testing.assert_array_equal(AH.data, ref.data)
