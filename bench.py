@@ -521,6 +521,71 @@ def run_driven(args):
     print(json.dumps(out))
 
 
+def run_hubbard(args):
+    """Fermion workload: spinful Fermi-Hubbard 4x4 periodic, N_up = N_down = 5,
+    t = 1, U = 4, (kx, ky) = (0, 0), complex128 CSR.  Lanczos lowest
+    eigenpairs with full reorthogonalisation (FP64, and mixed: complex64
+    matrix values with FP64 vectors and recurrences), then the quench of the
+    ground state to U = 8 over t in [0, 10] in 100 expm_multiply steps
+    (FP64 and mixed)."""
+    import torch
+    from quspin_gb300 import hamiltonian, spinful_fermion_basis_general
+    from quspin_gb300.tools import ExpmMultiplyParallel, lanczos_full, lin_comb_Q_T
+    Lx = Ly = 4
+    N = Lx * Ly
+    s_ = np.arange(N)
+    X, Y = s_ % Lx, s_ // Lx
+    tx, ty = (X + 1) % Lx + Y * Lx, X + ((Y + 1) % Ly) * Lx
+    t0 = time.perf_counter()
+    b = spinful_fermion_basis_general(N, Nf=(5, 5), kx=(tx, 0), ky=(ty, 0))
+    hop = [[-1.0, i, tx[i]] for i in range(N)] + [[-1.0, i, ty[i]] for i in range(N)]
+    hopc = [[1.0, i, tx[i]] for i in range(N)] + [[1.0, i, ty[i]] for i in range(N)]
+
+    def ham(U):
+        st = [["+-|", hop], ["-+|", hopc], ["|+-", hop], ["|-+", hopc], ["n|n", [[U, i, i] for i in range(N)]]]
+        return hamiltonian(st, [], basis=b, dtype=np.complex128)
+    H4, H8 = ham(4.0), ham(8.0)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    v0 = torch.tensor(rng.normal(size=b.Ns) + 0j, device="cuda")
+    m = 150
+    res = {}
+    for prec in ("double", "mixed"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, V, Q = lanczos_full(H4, v0, m, reorth=True, precision=prec)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        g = lin_comb_Q_T(V[:, 0], Q)
+        g = g / torch.linalg.vector_norm(g)
+        res[prec] = {"E": E[:4].tolist(), "seconds": el, "ground": g}
+    psi0 = res["double"]["ground"]
+    e_err = [abs(a - b_) for a, b_ in zip(res["mixed"]["E"], res["double"]["E"])]
+    st_err = float(torch.linalg.vector_norm(res["mixed"]["ground"] * torch.vdot(res["mixed"]["ground"], psi0).sgn().conj()
+                                            - psi0))
+    # quench: 100 steps of dt = 0.1 under U = 8
+    q = {}
+    A8 = H8.tocsr_gpu()
+    for prec in ("double", "mixed"):
+        op = ExpmMultiplyParallel(A8, a=-0.1j, precision=prec)
+        F = psi0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(100):
+            op.dot(F, overwrite_v=True)
+        torch.cuda.synchronize()
+        q[prec] = {"seconds": time.perf_counter() - t0, "F": F}
+    q_err = float(torch.linalg.vector_norm(q["mixed"]["F"] - q["double"]["F"]) / torch.linalg.vector_norm(q["double"]["F"]))
+    out = {"workload": "hubbard_4x4_Nf5_5_k00", "Ns": b.Ns, "nnz": int(H4.tocsr_gpu().nnz), "build_s": t_build,
+           "lanczos_m": m, "lanczos_fp64": {"E0..3": res["double"]["E"], "seconds": res["double"]["seconds"]},
+           "lanczos_mixed": {"E0..3": res["mixed"]["E"], "seconds": res["mixed"]["seconds"],
+                             "abs_energy_error_vs_fp64": e_err, "ground_state_error_vs_fp64": st_err},
+           "quench_fp64_seconds": q["double"]["seconds"], "quench_mixed_seconds": q["mixed"]["seconds"],
+           "quench_mixed_rel_state_error_vs_fp64": q_err}
+    print(json.dumps(out))
+
+
 def run_reference(args, rank, ws):
     """The reference's CPU path (the oracle port of QuSpin's OpenMP basis,
     CSR assembly and Taylor loop) on the host cores; each step a bounded
@@ -581,7 +646,7 @@ def main():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
     p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
-    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven"],
+    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard"],
                    help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
     if args.L != 32 and args.workload == "j1j2":
@@ -594,6 +659,9 @@ def main():
         return
     if args.workload == "driven":
         run_driven(args)
+        return
+    if args.workload == "hubbard":
+        run_hubbard(args)
         return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")

@@ -62,18 +62,26 @@ def fragment_3_1(norm_info, n0, tol, m_max=55, ell=2):
 
 
 class LazyOperatorNormInfo:
-    """Exact 1-norm of a(A - mu I) and lazy onenormest of its powers
-    (html :399-463); the products run on the device."""
+    """Exact 1-norm of a(A - mu I) and lazy 1-norm estimates of its powers
+    (html :399-463).
 
-    def __init__(self, apply, apply_h, n, A_1_norm, a, dtype, ell=2):
-        self._apply = apply          # host (n, k) -> host (n, k):  a (A - mu) x
-        self._apply_h = apply_h      # host (n, k) -> host (n, k):  conj(a) (A^H - conj mu) x
+    ``apply`` / ``apply_h`` map an [n, k] block to a (A - mu I) X and
+    conj(a) (A^H - conj(mu) I) X.  With ``device`` (an [n, k] block dtype and
+    torch device) the products and the estimator run on device tensors
+    (``_onenormest.onenormest_device``); otherwise they take host arrays and
+    scipy's ``onenormest`` drives them.
+    """
+
+    def __init__(self, apply, apply_h, n, A_1_norm, a, dtype, ell=2, device=None):
+        self._apply = apply
+        self._apply_h = apply_h
         self._n = n
         self._a = a
         self._dtype = dtype
         self._A_1_norm = A_1_norm
         self._ell = ell
         self._d = {}
+        self._device = device
         self.matvecs = 0
 
     def onenorm(self):
@@ -94,9 +102,26 @@ class LazyOperatorNormInfo:
                               rmatmat=rmv)
 
     def d(self, p):
-        from scipy.sparse.linalg import onenormest
         if p not in self._d:
-            est = onenormest(self._linop() ** p)
+            if self._device is not None:
+                from ._onenormest import onenormest_device
+                tdtype, dev = self._device
+
+                def mm(X, f=self._apply):
+                    for _ in range(p):
+                        X = f(X)
+                        self.matvecs += 1
+                    return X
+
+                def rmm(X, f=self._apply_h):
+                    for _ in range(p):
+                        X = f(X)
+                        self.matvecs += 1
+                    return X
+                est = onenormest_device(mm, rmm, self._n, tdtype, dev, t=self._ell)
+            else:
+                from scipy.sparse.linalg import onenormest
+                est = onenormest(self._linop() ** p)
             self._d[p] = est ** (1.0 / p)
         return self._d[p]
 

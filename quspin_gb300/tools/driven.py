@@ -97,15 +97,15 @@ class DrivenEvolution:
             aa, mm = (np.conj(a), np.conj(mu)) if conj else (a, mu)
             MM = M.conj_transpose() if conj else M
 
-            def f(v):
-                x = D.to_device(np.asarray(v), np.complex128)
-                x2 = x.reshape(x.shape[0], -1).contiguous()
+            def f(X):
+                x2 = X.reshape(X.shape[0], -1).to(torch.complex128).contiguous()
                 y = torch.empty_like(x2)
                 MM.matvec_into(x2, y, a=aa, overwrite=True)
                 y.sub_(x2, alpha=aa * mm)
-                return D.to_host(y.reshape(x.shape))
+                return y.reshape(X.shape)
             return f
-        info = LazyOperatorNormInfo(apply(False), apply(True), self.n, A1, a, np.dtype(np.complex128))
+        info = LazyOperatorNormInfo(apply(False), apply(True), self.n, A1, a, np.dtype(np.complex128),
+                                    device=(torch.complex128, D.device()))
         return fragment_3_1(info, 1, tol, ell=2)
 
     def _taylor(self, F, M, mu, a, m, s):
@@ -140,7 +140,7 @@ class DrivenEvolution:
                     self._taylor(F, M, mu, a, int(m_pred[i]), int(s_pred[i]))
                     if record is not None:
                         record.append((int(m_pred[i]), int(s_pred[i])))
-                nonconv = int(self._ctl[5].view(torch.int32)[0].item())
+                nonconv = int(self._ctl.view(torch.int32)[10].item())
                 if nonconv:
                     self.fallbacks += 1
                     F.copy_(saved)

@@ -121,6 +121,7 @@ class ExpmMultiplyParallel:
 
     # -- (m*, s) ---------------------------------------------------------------
     def _shifted_apply(self, conj):
+        """Device map X -> a (A - mu I) X (or its adjoint) on [n, k] blocks."""
         a = complex(self._a)
         mu = complex(self._mu)
         if conj:
@@ -131,14 +132,12 @@ class ExpmMultiplyParallel:
         else:
             M = self._Ad
 
-        def f(v):
-            v = np.asarray(v)
-            x = D.to_device(v, np.complex128)
-            x2 = x.reshape(x.shape[0], -1).contiguous()
+        def f(X):
+            x2 = X.reshape(X.shape[0], -1).to(torch.complex128).contiguous()
             y = torch.empty_like(x2)
             M.matvec_into(x2, y, a=a, overwrite=True)
             y.sub_(x2, alpha=a * mu)
-            return D.to_host(y.reshape(x.shape))
+            return y.reshape(X.shape)
         return f
 
     def _calculate_partition(self):
@@ -147,7 +146,8 @@ class ExpmMultiplyParallel:
         else:
             self._norm_info = LazyOperatorNormInfo(self._shifted_apply(False), self._shifted_apply(True),
                                                    self._Ad.shape[0], self._A_1_norm, self._a,
-                                                   np.dtype(np.complex128), ell=2)
+                                                   np.dtype(np.complex128), ell=2,
+                                                   device=(torch.complex128, D.device()))
             self._m_star, self._s = fragment_3_1(self._norm_info, 1, self._tol, ell=2)
 
     # -- application -------------------------------------------------------------
@@ -206,7 +206,7 @@ class ExpmMultiplyParallel:
         """Substeps of the last dot that used all m* terms without the
         stopping test firing (reads the device counter)."""
         c = getattr(self, "_last_ctl", None)
-        return 0 if c is None else int(c[5].view(torch.int32)[0].item())
+        return 0 if c is None else int(c.view(torch.int32)[10].item())
 
     @property
     def terms_executed(self):

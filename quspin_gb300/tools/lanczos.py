@@ -25,10 +25,22 @@ __all__ = ["lanczos_full", "lanczos_iter", "lin_comb_Q_T", "expm_lanczos"]
 
 
 class _DeviceOp:
-    """Uniform device product y = A x for the operators this package knows."""
+    """Uniform device product y = A x for the operators this package knows.
+    precision="mixed" applies float32 / complex64 matrix values to the FP64
+    vectors (the recurrence itself stays FP64)."""
 
-    def __init__(self, A):
+    def __init__(self, A, precision="double"):
         from ..operators import hamiltonian, quantum_LinearOperator
+        if precision == "mixed":
+            if isinstance(A, hamiltonian):
+                A = A.tocsr_gpu()
+            if isinstance(A, (DeviceCSR, DeviceDIA)):
+                dt = np.dtype(A.dtype)
+                A0 = A
+                A = A.astype(np.float32 if dt.kind == "f" else np.complex64)
+                self.dtype = dt
+            else:
+                raise TypeError("precision='mixed' needs a hamiltonian or a device matrix")
         self.A = A
         if isinstance(A, (DeviceCSR, DeviceDIA)):
             self._f = lambda x, y: A.matvec_into(x, y, overwrite=True)
@@ -43,7 +55,8 @@ class _DeviceOp:
             self._f = lambda x, y: M.matvec_into(x, y, overwrite=True)
         else:
             raise TypeError("A must be a hamiltonian, quantum_LinearOperator or (sparse) matrix")
-        self.dtype = np.dtype(A.dtype)
+        if precision != "mixed":
+            self.dtype = np.dtype(A.dtype)
 
     def __call__(self, x, y):
         self._f(x, y)
@@ -118,13 +131,13 @@ def _start_vector(v0, dtype, eps):
     return q
 
 
-def lanczos_full(A, v0, m, full_ortho=False, out=None, eps=None, reorth=False):
+def lanczos_full(A, v0, m, full_ortho=False, out=None, eps=None, reorth=False, precision="double"):
     """(E, V, Q_T) of an m-step Lanczos run (_lanczos_utils.py:77-227)."""
     host = not D.is_device_array(v0)
     v0a = np.asanyarray(v0) if host else v0
     n = v0a.shape[0] if v0a.ndim else 1
     vdt = v0a.dtype if host else D.np_dtype(v0a.dtype)
-    op = _DeviceOp(A)
+    op = _DeviceOp(A, precision)
     dtype = np.result_type(op.dtype, vdt)
     if v0a.ndim != 1:
         raise ValueError("expecting array with ndim=1 for initial Lanczos vector.")

@@ -21,7 +21,12 @@ def _c1_like(L=14):
 
 
 def test_partition_and_shift_match_oracle(cuda):
+    """mu and the exact 1-norm match the oracle; (m*, s) match exactly when
+    the exact norm decides (condition 3.13); in the estimator branch the
+    estimates are random (the reference draws from the unseeded global
+    generator), so the chosen cost m* s must agree within 25%."""
     from quspin_gb300.tools import ExpmMultiplyParallel
+    from quspin_gb300.tools._partition import condition_3_13
     H = _c1_like()
     A = H.tocsr()
     for a in (-1j, -0.3j, -5j, -0.1):
@@ -31,7 +36,10 @@ def test_partition_and_shift_match_oracle(cuda):
         o = O.ExpmMultiplyParallelOracle(A, a=a)
         assert abs(complex(g._mu) - complex(o._mu)) < 1e-13
         assert abs(g._A_1_norm - o._A_1_norm) < 1e-12 * o._A_1_norm
-        assert (g._m_star, g._s) == (o._m_star, o._s)
+        if condition_3_13(abs(a) * o._A_1_norm, 1, 55, 2):
+            assert (g._m_star, g._s) == (o._m_star, o._s)
+        else:
+            assert abs(g._m_star * g._s - o._m_star * o._s) <= 0.25 * o._m_star * o._s
 
 
 @pytest.mark.parametrize("a", [-1j, -0.5, -5j])

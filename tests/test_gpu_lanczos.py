@@ -89,3 +89,15 @@ def test_complex_start_vector(cuda):
     # early steps, before loss of orthogonality amplifies rounding differences
     np.testing.assert_allclose(E, Eo, rtol=0, atol=1e-10)
     np.testing.assert_allclose(np.abs(Q), np.abs(Qo), rtol=0, atol=1e-10)
+
+
+def test_mixed_precision_lanczos(cuda):
+    """complex64 / float32 matrix values with FP64 vectors and recurrence:
+    ground energy within 1e-6 of the FP64 run."""
+    from quspin_gb300.tools import lanczos_full
+    H = _H(16)
+    rng = np.random.default_rng(5)
+    v0 = rng.normal(size=H.Ns)
+    E64 = lanczos_full(H, v0, 60, reorth=True)[0]
+    E32 = lanczos_full(H, v0, 60, reorth=True, precision="mixed")[0]
+    assert abs(E64[0] - E32[0]) < 1e-6 * max(1.0, abs(E64[0]))
