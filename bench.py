@@ -184,41 +184,49 @@ def spmv_bytes(n, nnz, nvec=1):
 
 def time_kernels(op, F, reps=20):
     """Average device time of the Taylor-term kernel launched alone (stopping
-    test disabled) and of the plain SpMV, CUDA events on the launching stream."""
+    test disabled) in the operator's precision and in IEEE double, and of the
+    plain SpMV; CUDA events on the launching stream."""
     import torch
     from quspin_gb300 import _device as D
     from quspin_gb300 import _lib
+    from quspin_gb300.tune import tune_taylor
     A = op.A_device
     n = A.shape[0]
     st = torch.cuda.current_stream()
-    work = torch.empty(2 * n, dtype=torch.complex128, device=F.device)
-    b0, b1 = work[:n], work[n:]
-    b0.copy_(F)
-    Fw = F.clone()
-    ctl = torch.zeros(6, dtype=torch.int64, device=F.device)
-    ctl.view(torch.float64)[0] = float("inf")          # c1 = inf: the stopping test never fires
-    coeff = torch.tensor([complex(op.a) / 1000.0], dtype=torch.complex128, device=F.device)
     mu = complex(op._mu)
+    one = torch.ones(1, dtype=torch.complex128, device=F.device)
 
-    from quspin_gb300.tune import tune_taylor
-    group = tune_taylor(A, 1, _lib.C128)
+    def term_time(M, btype):
+        work = torch.empty(2 * n, dtype=torch.complex64 if btype == _lib.C64 else torch.complex128, device=F.device)
+        b0, b1 = work[:n], work[n:]
+        Fw = F.clone()
+        ctl = torch.zeros(6, dtype=torch.int64, device=F.device)
+        _lib.call("qs_taylor_rescale", n, 1, D.ptr(Fw), D.ptr(b0), btype, D.ptr(one), D.ptr(ctl), 0, D.stream())
+        ctl.view(torch.float64)[0] = float("inf")          # c1 = inf and tol = 0: the stopping test never fires
+        coeff = torch.tensor([complex(op.a) / 1000.0], dtype=torch.complex128, device=F.device)
+        group = tune_taylor(M, 1, btype)
 
-    def launch(j):
-        bi, bo = (b0, b1) if j % 2 == 0 else (b1, b0)
-        _lib.call("qs_taylor_term", n, A.nnz, D.ptr(A.indptr), A.idx64, D.ptr(A.indices), D.ptr(A.data),
-                  D.code(A.dtype), D.ptr(bi), D.ptr(bo), _lib.C128, D.ptr(Fw), 1, mu.real, mu.imag, D.ptr(coeff),
-                  0, 0.0, D.ptr(ctl), group, D.stream())
-    for j in range(3):
-        launch(j)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for j in range(reps):
-        launch(j)
-    e1.record(st)
-    torch.cuda.synchronize()
-    t_term = e0.elapsed_time(e1) / 1e3 / reps
+        def launch(j):
+            bi, bo = (b0, b1) if j % 2 == 0 else (b1, b0)
+            _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
+                      M.vcode, D.ptr(bi), D.ptr(bo), btype, D.ptr(Fw), 1, mu.real, mu.imag, D.ptr(coeff),
+                      0, 0.0, D.ptr(ctl), group, D.stream())
+        for j in range(3):
+            launch(j)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for j in range(reps):
+            launch(j)
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps, group
+
+    M, bt = op._operand()
+    t_term, group = term_time(M, bt)
+    t_ieee, group_ieee = term_time(A, _lib.C128)
     y = torch.empty_like(F)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for _ in range(3):
         A.matvec_into(F, y)
     torch.cuda.synchronize()
@@ -228,7 +236,7 @@ def time_kernels(op, F, reps=20):
     e1.record(st)
     torch.cuda.synchronize()
     t_spmv = e0.elapsed_time(e1) / 1e3 / reps
-    return t_term, t_spmv, group
+    return t_term, t_spmv, group, t_ieee, group_ieee
 
 
 def cpu_baseline(H, op, terms_per_evolution, budget_s=12.0):
@@ -318,23 +326,45 @@ def run_ours(args, rank, ws):
     torch.cuda.synchronize()
     T_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
     norm_err = abs(np.linalg.norm(w_host) - 1.0)
-    t_term, t_spmv, group = time_kernels(op, v_dev)
+    # the same evolution with IEEE double products: throughput and state error
+    F_pair = F.clone()
+    op.precision = "ieee"
+    F.copy_(v_dev)
+    op.run_device(F)
+    torch.cuda.synchronize()
+    e0.record(st)
+    steps_ieee = max(1, min(args.steps, 3))
+    for _ in range(steps_ieee):
+        F.copy_(v_dev)
+        op.run_device(F)
+    e1.record(st)
+    torch.cuda.synchronize()
+    T_ieee = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
+    rel_err = float(torch.linalg.vector_norm(F_pair - F) / torch.linalg.vector_norm(F))
+    op.precision = "double"
+    t_term, t_spmv, group, t_ieee, group_ieee = time_kernels(op, v_dev)
     peak, peak_kind = peak_hbm()
     tb = taylor_term_bytes(n, nnz)
     achieved = tb / t_term / 1e9
-    launches_per_evolution = 2 + op.s * (op.m_star + 1)   # rescale + s (m* terms + rescale); copy excluded
+    # rescale (norm + load) + s (m* terms + norm + load); copy excluded
+    launches_per_evolution = 2 + op.s * (op.m_star + 2)
     out = {
         "metric": "expm_multiply evolutions/s", "value": ws * args.steps / T, "unit": "evolutions/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (partial sums, shift, stopping test) with f32-pair products",
         "data": "synthetic (seeded Gaussian state; Hamiltonian exactly as configured)",
         "config": dict(W, Ns=n, nnz=nnz, m_star=op.m_star, s=op.s, terms_per_evolution=terms,
                        parallelism="replicas" if ws > 1 else "single", build_s=round(t_build, 3),
-                       expm_setup_s=round(t_setup, 3)),
+                       expm_setup_s=round(t_setup, 3), precision="double (float-pair products)"),
+        "ieee_fp64": {"value": ws * steps_ieee / T_ieee, "unit": "evolutions/s", "taylor_term_ms": 1e3 * t_ieee,
+                      "launch_shape": {"lanes_per_row": group_ieee & 0xff,
+                                       "entries_in_flight": (group_ieee >> 8) & 0xff},
+                      "rel_state_error_of_value_path": rel_err},
         "e2e": {"value": ws * args.steps / T_e2e, "unit": "evolutions/s", "h2d_bytes_per_step": int(n * 16),
                 "d2h_bytes_per_step": int(n * 16)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_term_kernel",
+                     "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_lp_kernel",
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
                      "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff},
                      "spmv_gbs": spmv_bytes(n, nnz) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv},
@@ -382,6 +412,7 @@ def run_sectors(args):
     mats = ising_sector_mats(L)
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
+    print("sectors built in {:.1f} s".format(t_build), file=sys.stderr, flush=True)
     rng = np.random.default_rng(0)
     blocks = []
     for M in mats:
@@ -390,7 +421,9 @@ def run_sectors(args):
     st = torch.cuda.current_stream()
     ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     # plain per-block FP64 loop
+    t0 = time.perf_counter()
     plain = [ExpmMultiplyParallel(M, a=-1j * T) for M in mats]
+    print("per-sector partitions in {:.1f} s".format(time.perf_counter() - t0), file=sys.stderr, flush=True)
     outs = [None] * len(mats)
 
     def plain_step():
@@ -406,6 +439,7 @@ def run_sectors(args):
     e1.record(st)
     torch.cuda.synchronize()
     t_plain = e0.elapsed_time(e1) / 1e3 / args.steps
+    print("plain loop {:.3f} s per step".format(t_plain), file=sys.stderr, flush=True)
     ref = [o.clone() for o in outs]
     res = {}
     for prec in ("double", "mixed"):
@@ -442,8 +476,10 @@ def run_driven(args):
     w=2 pi; 32 seeded states; 200 piecewise-constant steps per period.
     Plain per-step selection (exact 1-norm + fragment 3.1) vs the learned
     predictor (trained here on the plain method's labels for (h0, A, w) drawn
-    within +-30%), both on the batched FP64 path; plus the plain selection
-    applied one state at a time (the unbatched FP64 path)."""
+    within +-30%) on the batched path in IEEE double, float-pair and complex64
+    arithmetic; plus the plain selection applied one state at a time in IEEE
+    double (the plain FP64 method), the base of the reported speed-ups.
+    State errors are against the batched IEEE plain run."""
     import torch
     from quspin_gb300 import hamiltonian, spin_basis_general
     from quspin_gb300.learned import PartitionPredictor
@@ -482,26 +518,31 @@ def run_driven(args):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     H = ham(h0, A, w)
-    ev = DrivenEvolution(H, nvec=k)
     V = rng.normal(size=(H.Ns, k)) + 1j * rng.normal(size=(H.Ns, k))
     V /= np.linalg.norm(V, axis=0)
     V0 = torch.tensor(V, device="cuda")
     res = {}
-    for mode in ("plain", "learned"):
+    # (label, selection, arithmetic): the reference arithmetic first (the
+    # error reference), then the float-pair and complex64 forms
+    for label, mode, prec in (("plain_batched_ieee", "plain", "ieee"), ("plain_batched", "plain", "double"),
+                              ("learned_batched", "learned", "double"),
+                              ("learned_batched_mixed", "learned", "mixed")):
+        ev = DrivenEvolution(H, nvec=k, precision=prec)
         F = V0.clone()
-        ev.fallbacks = 0
-        ev.norm_passes = 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ev.run(F, 0.0, dt, nsteps, mode=mode, predictor=pred, segment=100)
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
-        res[mode] = {"seconds": el, "state_evolutions_per_s": k * nsteps / el, "norm_passes": ev.norm_passes,
-                     "fallback_segments": ev.fallbacks, "F": F}
-    err = float(torch.linalg.vector_norm(res["learned"]["F"] - res["plain"]["F"]) /
-                torch.linalg.vector_norm(res["plain"]["F"]))
-    # unbatched plain: one state at a time, a few steps, scaled
-    ev1 = DrivenEvolution(H, nvec=1)
+        res[label] = {"seconds": el, "state_evolutions_per_s": k * nsteps / el, "norm_passes": ev.norm_passes,
+                      "fallback_segments": ev.fallbacks, "precision": prec, "F": F}
+        print(label, "{:.1f} s".format(el), file=sys.stderr, flush=True)
+    Fref = res["plain_batched_ieee"]["F"]
+    for label in res:
+        res[label]["rel_state_error_vs_ieee_plain"] = float(
+            torch.linalg.vector_norm(res[label]["F"] - Fref) / torch.linalg.vector_norm(Fref))
+    # the plain FP64 GPU method: one state at a time, IEEE products, plain selection
+    ev1 = DrivenEvolution(H, nvec=1, precision="ieee")
     F1 = V0[:, :1].clone().contiguous()
     n1 = min(nsteps, 100)
     torch.cuda.synchronize()
@@ -509,15 +550,16 @@ def run_driven(args):
     ev1.run(F1, 0.0, dt, n1, mode="plain")
     torch.cuda.synchronize()
     el1 = time.perf_counter() - t0
+    base = n1 / el1
     out = {"metric": "expm_multiply evolutions/s", "workload": "driven_ising_L{}_k0_p0_32_states_{}_periods".format(
         L, periods), "unit": "state-steps/s (one state through one piecewise step)",
-        "Ns": H.Ns, "steps": nsteps, "dt": dt,
-        "plain_batched": {x: y for x, y in res["plain"].items() if x != "F"},
-        "learned_batched": {x: y for x, y in res["learned"].items() if x != "F"},
-        "plain_unbatched": {"state_evolutions_per_s": n1 / el1, "sample_steps": n1},
-        "learned_vs_plain_rel_state_error": err,
-        "training": {"samples": int(len(ms)), "label_seconds": t_data, "train_seconds": t_train,
-                     "final_loss": hist[-1], "first_loss": hist[0]}}
+        "Ns": H.Ns, "steps": nsteps, "dt": dt}
+    for label, r in res.items():
+        out[label] = {x: y for x, y in r.items() if x != "F"}
+        out[label]["speedup_vs_plain_unbatched_ieee"] = r["state_evolutions_per_s"] / base
+    out["plain_unbatched_ieee"] = {"state_evolutions_per_s": base, "sample_steps": n1}
+    out["training"] = {"samples": int(len(ms)), "label_seconds": t_data, "train_seconds": t_train,
+                       "final_loss": hist[-1], "first_loss": hist[0]}
     print(json.dumps(out))
 
 

@@ -8,7 +8,9 @@
  *   -1 invalid argument, -2 CUDA error, -3 unknown operator character,
  *   -4 complex element in a real dtype, -5 buffer too small,
  *   -6 unsupported configuration, -7 iteration cap reached.
- * Element type codes: 0 float32, 1 float64, 2 complex64, 3 complex128.
+ * Element type codes: 0 float32, 1 float64, 2 complex64, 3 complex128,
+ * 4 real value as a float pair hi + lo (8 bytes), 5 complex value as two
+ * float pairs {re.hi, re.lo, im.hi, im.lo} (16 bytes).
  *
  * Each declaration names the reference interface it replaces (QuSpin 1.0.1;
  * paths relative to the reference project root; "html" = the Sphinx
@@ -109,6 +111,13 @@ int qs_inplace_op(void *sym, const void *d_states, const uint32_t *d_norms, int6
 int qs_csr_matvec(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                   const void *d_data, int dtype, const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re,
                   double a_im, int overwrite, int group, void *stream);
+/* Paired-single form of qs_csr_matvec for float64 / complex128 x and y: the
+ * values split by qs_split_pairs (pdtype 4 / 5), x scaled by a power of two
+ * and split into d_xs (n*nvec*8 or 16 bytes of scratch; d_norm: 8 bytes),
+ * products and row sums in FP32 instructions with 48-bit significands. */
+int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                        const void *d_pdata, int pdtype, const void *d_x, int xtype, void *d_y, int64_t nvec,
+                        double a_re, double a_im, int overwrite, int group, void *d_xs, void *d_norm, void *stream);
 int qs_dia_matvec(int64_t n, int ndiag, const int64_t *d_offsets, int64_t ldd, const void *d_data, int dtype,
                   const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re, double a_im, int overwrite,
                   void *stream);
@@ -129,6 +138,11 @@ int qs_csr_1_norm(int64_t n, const void *d_indptr, int idx64, const int32_t *d_i
 /* ---- _wrapper_expm_multiply / _wrapper_expm_multiply_batch
  * (html expm_multiply_parallel_core.html:347-372) ----------------------- */
 int qs_expm_ctl_bytes(void);
+/* Taylor-term storage (btype): 3 = complex128 with IEEE double products;
+ * 5 = float pairs with FP32-instruction products (values from qs_split_pairs,
+ * dtype 4 / 5); 2 = complex64 with float32 / complex64 values.  F, the
+ * shift, the coefficients and the stopping test are double in all three. */
+int qs_split_pairs(int64_t count, const double *d_src, void *d_dst, void *stream);
 int qs_taylor_term(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                    const void *d_data, int dtype, const void *d_Bin, void *d_Bout, int btype, void *d_F,
                    int64_t nvec, double mu_re, double mu_im, const void *d_coeff, int j, double tol, void *d_ctl,

@@ -18,7 +18,7 @@ _lib = None
 _lock = threading.Lock()
 
 # element type codes shared with the C side
-F32, F64, C64, C128 = 0, 1, 2, 3
+F32, F64, C64, C128, PF, CPF = 0, 1, 2, 3, 4, 5
 
 STATUS = {
     -1: "invalid argument",
@@ -61,6 +61,8 @@ _SIGS = {
     "qs_inplace_op": (_i, [_vp, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _vp,
                            _vp, _i64, _vp, _vp]),
     "qs_csr_matvec": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp]),
+    "qs_csr_matvec_pairs": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp, _vp,
+                                 _vp]),
     "qs_dia_matvec": (_i, [_i64, _i, _vp, _i64, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _vp]),
     "qs_reduce_scratch_doubles": (_i, []),
     "qs_vdot": (_i, [_i64, _vp, _vp, _i, _vp, _vp, _vp]),
@@ -68,6 +70,7 @@ _SIGS = {
     "qs_csr_trace": (_i, [_i64, _vp, _i, _vp, _vp, _i, _vp, _vp, _vp]),
     "qs_csr_1_norm": (_i, [_i64, _vp, _i, _vp, _vp, _i, _d, _d, _vp, _vp, _vp, _vp]),
     "qs_expm_ctl_bytes": (_i, []),
+    "qs_split_pairs": (_i, [_i64, _vp, _vp, _vp]),
     "qs_taylor_term": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _d, _d, _vp, _i, _d, _vp,
                             _i, _vp]),
     "qs_taylor_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp]),

@@ -20,23 +20,15 @@
 // accumulate into F and both infinity norms (row sums of moduli over the k
 // right-hand sides).  The last block of each launch evaluates the stopping
 // test in a small device control block, so the host never synchronises;
-// launches after the test has fired return immediately.  B may be stored in
-// complex64 (the mixed form) while F, mu, the coefficients and the norms stay
-// in double precision.
+// launches after the test has fired return immediately.  The kernels here do
+// every product in IEEE double (the "ieee" form); csrc/expm_lp.cu holds the
+// paired-single and complex64 forms of the same term, selected by btype.
 #include "qs_common.cuh"
-
-struct ExpmCtl {
-    double c1;                 // ||B||_inf at the start of the current term
-    unsigned long long c2;     // running max row-norm of the new term (bits of a double >= 0)
-    unsigned long long fn;     // running max row-norm of F
-    int done;                  // stopping test fired in this substep
-    unsigned int arrive;       // blocks finished in the current launch
-    long long terms;           // Taylor terms executed so far
-    int nonconv;               // substeps that used all m* terms without the test firing
-    int pad;
-};
+#include "expm_ctl.cuh"
 
 extern "C" int qs_expm_ctl_bytes() { return (int)sizeof(ExpmCtl); }
+extern "C" int qs_multi_ctl_bytes() { return (int)sizeof(MultiCtl); }
+extern "C" int qs_max_sectors() { return QS_MAX_SECTORS; }
 
 template <typename T> struct BLoad;
 template <> struct BLoad<cdbl> {
@@ -46,26 +38,12 @@ template <> struct BLoad<cdbl> {
     }
     __device__ static void st(cdbl *p, int64_t i, cdbl v) { p[i] = v; }
 };
-template <> struct BLoad<cflt> {
-    __device__ static cdbl ld(const cflt *p, int64_t i) {
-        float2 v = __ldg(reinterpret_cast<const float2 *>(p) + i);
-        return cdbl{(double)v.x, (double)v.y};
-    }
-    __device__ static void st(cflt *p, int64_t i, cdbl v) { p[i] = cflt{(float)v.x, (float)v.y}; }
-};
 template <typename T> struct DLoad;
 template <> struct DLoad<double> { __device__ static double ld(const double *p, int64_t i) { return __ldg(p + i); } };
-template <> struct DLoad<float> { __device__ static double ld(const float *p, int64_t i) { return (double)__ldg(p + i); } };
 template <> struct DLoad<cdbl> {
     __device__ static cdbl ld(const cdbl *p, int64_t i) {
         double2 v = __ldg(reinterpret_cast<const double2 *>(p) + i);
         return cdbl{v.x, v.y};
-    }
-};
-template <> struct DLoad<cflt> {
-    __device__ static cdbl ld(const cflt *p, int64_t i) {
-        float2 v = __ldg(reinterpret_cast<const float2 *>(p) + i);
-        return cdbl{(double)v.x, (double)v.y};
     }
 };
 
@@ -76,7 +54,7 @@ __device__ __forceinline__ void madd(cdbl &acc, cdbl d, cdbl x)
     acc.y += d.x * x.y + d.y * x.x;
 }
 
-__device__ __forceinline__ double cabs_(cdbl v) { return sqrt(v.x * v.x + v.y * v.y); }
+__device__ __forceinline__ double cabs_(cdbl v) { return hypot(v.x, v.y); }
 
 // F and the new term are touched once per term: stream them (evict-first)
 // so the gathered vector keeps its place in L2.
@@ -87,40 +65,6 @@ __device__ __forceinline__ cdbl ldF(const cdbl *p)
 }
 __device__ __forceinline__ void stF(cdbl *p, cdbl v) { __stcs(reinterpret_cast<double2 *>(p), make_double2(v.x, v.y)); }
 __device__ __forceinline__ void stB(cdbl *p, cdbl v) { __stcs(reinterpret_cast<double2 *>(p), make_double2(v.x, v.y)); }
-__device__ __forceinline__ void stB(cflt *p, cdbl v) { __stcs(reinterpret_cast<float2 *>(p), make_float2((float)v.x, (float)v.y)); }
-
-// block-wide max of two non-negative doubles, atomically folded into ctl
-__device__ __forceinline__ void fold_max2(double a, double b, unsigned long long *ga, unsigned long long *gb)
-{
-    __shared__ double sa[32], sb[32];
-    for (int o = 16; o > 0; o >>= 1) {
-        a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
-        b = fmax(b, __shfl_down_sync(0xffffffffu, b, o));
-    }
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) { sa[w] = a; sb[w] = b; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double ma = 0.0, mb = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { ma = fmax(ma, sa[k]); mb = fmax(mb, sb[k]); }
-        if (ga) atomicMax(ga, (unsigned long long)__double_as_longlong(ma));
-        if (gb) atomicMax(gb, (unsigned long long)__double_as_longlong(mb));
-    }
-}
-
-// returns true in thread 0 of the last block to arrive
-__device__ __forceinline__ bool last_block(ExpmCtl *ctl)
-{
-    __shared__ bool is_last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned int t = atomicAdd(&ctl->arrive, 1u);
-        is_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    return is_last;
-}
 
 template <typename T> __device__ __forceinline__ T st_ld(const T *p) { return __ldcs(p); }
 template <> __device__ __forceinline__ cdbl st_ld<cdbl>(const cdbl *p)
@@ -128,20 +72,11 @@ template <> __device__ __forceinline__ cdbl st_ld<cdbl>(const cdbl *p)
     double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
     return cdbl{v.x, v.y};
 }
-template <> __device__ __forceinline__ cflt st_ld<cflt>(const cflt *p)
-{
-    float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
-    return cflt{v.x, v.y};
-}
 __device__ __forceinline__ double wid(double v) { return v; }
-__device__ __forceinline__ double wid(float v) { return (double)v; }
 __device__ __forceinline__ cdbl wid(cdbl v) { return v; }
-__device__ __forceinline__ cdbl wid(cflt v) { return cdbl{(double)v.x, (double)v.y}; }
 template <typename T> __device__ __forceinline__ T zro();
 template <> __device__ __forceinline__ double zro<double>() { return 0.0; }
-template <> __device__ __forceinline__ float zro<float>() { return 0.0f; }
 template <> __device__ __forceinline__ cdbl zro<cdbl>() { return cdbl{0.0, 0.0}; }
-template <> __device__ __forceinline__ cflt zro<cflt>() { return cflt{0.0f, 0.0f}; }
 
 // G lanes per row, U independent entries per lane per step, NB right-hand
 // sides per pass (see csrc/sparse.cu for the row hand-out rule).
@@ -350,9 +285,10 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
     return term_nb<DT, BT, int32_t>(n, indptr, indices, data, Bin, Bout, F, nvec, mu, coeff, j, tol, ctl, G, U, st);
 }
 
-// One Taylor term (see file header).  dtype: value type of A (QS_F64,
-// QS_C128, QS_F32, QS_C64); btype: storage of B (QS_C128 or QS_C64); F is
-// complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
+// One Taylor term (see file header).  btype: storage of B -- QS_C128 (IEEE
+// double; dtype QS_F64 / QS_C128), QS_CPF (paired single; dtype QS_PF /
+// QS_CPF, values split by qs_split_pairs) or QS_C64 (dtype QS_F32 / QS_C64);
+// F is complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
 // ctl: device control block (qs_expm_ctl_bytes()).  group: launch shape,
 // G | (U << 8) (G lanes per row 2..32, U = 1, 2, 4 entries in flight per lane);
 // 0 picks G from nnz/n and U = 2.
@@ -372,24 +308,23 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
     ExpmCtl *c = reinterpret_cast<ExpmCtl *>(ctl);
     const cdbl *cf = reinterpret_cast<const cdbl *>(coeff);
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
+    if (lp_btype(btype)) {
+        LpTerm a{n, indptr, idx64, indices, data, dtype, Bin, Bout, btype, Fp, nvec, mu, nullptr, nullptr, cf, j, tol,
+                 ctl, G, U, st};
+        return lp_taylor_term(a, false);
+    }
     if (btype == QS_C128) {
         switch (dtype) {
         case QS_F64: return term_idx<double, cdbl>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
         case QS_C128: return term_idx<cdbl, cdbl>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
         default: return QS_ERR_ARG;
         }
-    } else if (btype == QS_C64) {
-        switch (dtype) {
-        case QS_F32: return term_idx<float, cflt>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
-        case QS_C64: return term_idx<cflt, cflt>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
-        case QS_F64: return term_idx<double, cflt>(idx64, n, indptr, indices, data, Bin, Bout, Fp, nvec, mu, cf, j, tol, c, G, U, st);
-        default: return QS_ERR_ARG;
-        }
     }
     return QS_ERR_ARG;
 }
 
-// F = eta F; B0 = F; c1 = ||F||_inf; done = 0 (eta: device complex128).
+// F = eta F; B0 = F (scaled by 2^-bexp for QS_CPF / QS_C64 storage);
+// c1 = ||F||_inf; done = 0 (eta: device complex128).
 // With eta = 1 and substep_end = 0 this is the set-up before the first
 // substep; with substep_end = 1 a substep whose stopping test never fired is
 // counted in the control block.
@@ -398,15 +333,14 @@ extern "C" int qs_taylor_rescale(int64_t n, int64_t nvec, void *F, void *B0, int
 {
     if (n < 1 || nvec < 1 || !F || !B0 || !eta || !ctl) return QS_ERR_ARG;
     cudaStream_t st = qs_stream(stream);
+    if (lp_btype(btype))
+        return lp_taylor_rescale(n, nvec, (cdbl *)F, B0, btype, (const cdbl *)eta, 1, nullptr, ctl, substep_end, false,
+                                 st);
+    if (btype != QS_C128) return QS_ERR_ARG;
     int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
     int blocks = (int)(b > cap ? cap : b);
-    if (btype == QS_C128)
-        taylor_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, (const cdbl *)eta,
-                                                           (ExpmCtl *)ctl, substep_end);
-    else if (btype == QS_C64)
-        taylor_rescale_kernel<cflt><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cflt *)B0, (const cdbl *)eta,
-                                                           (ExpmCtl *)ctl, substep_end);
-    else return QS_ERR_ARG;
+    taylor_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, (const cdbl *)eta,
+                                                       (ExpmCtl *)ctl, substep_end);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
@@ -422,7 +356,8 @@ extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int 
                                 void *work, int btype, void *ctl, int group, void *stream)
 {
     if (n < 1 || nvec < 1 || s < 1 || m_star < 0 || !work || !ctl) return QS_ERR_ARG;
-    size_t esz = btype == QS_C128 ? 16 : 8;
+    if (btype != QS_C128 && btype != QS_C64 && btype != QS_CPF) return QS_ERR_ARG;
+    size_t esz = btype == QS_C64 ? 8 : 16;
     char *b0 = reinterpret_cast<char *>(work);
     char *b1 = b0 + (size_t)n * nvec * esz;
     int rc = qs_taylor_rescale(n, nvec, F, b0, btype, one, ctl, 0, stream);
@@ -451,44 +386,6 @@ extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int 
 // mu_b, its own factor eta_b = exp(a mu_b / s) and its own stopping test on
 // the row sums of its block.  A sector whose test has fired is skipped by
 // the following launches of the substep.
-
-#define QS_MAX_SECTORS 64
-
-struct MultiCtl {
-    unsigned int arrive;
-    int nsec;
-    long long terms;                       // sector-terms executed
-    double c1[QS_MAX_SECTORS];
-    unsigned long long c2[QS_MAX_SECTORS];
-    unsigned long long fn[QS_MAX_SECTORS];
-    int done[QS_MAX_SECTORS];
-};
-
-extern "C" int qs_multi_ctl_bytes() { return (int)sizeof(MultiCtl); }
-extern "C" int qs_max_sectors() { return QS_MAX_SECTORS; }
-
-__device__ __forceinline__ int sector_of(const int64_t *soff, int nsec, int64_t r)
-{
-    int lo = 0, hi = nsec;          // largest b with soff[b] <= r
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (soff[mid] <= r) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ bool last_block_multi(MultiCtl *ctl)
-{
-    __shared__ bool is_last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned int t = atomicAdd(&ctl->arrive, 1u);
-        is_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    return is_last;
-}
 
 template <typename DT, typename BT, typename IT, int G, int NB, int U>
 __global__ void __launch_bounds__(256) taylor_multi_kernel(int64_t n, const IT *__restrict__ indptr,
@@ -685,8 +582,8 @@ static int multi_nb(int64_t n, const void *indptr, const int32_t *indices, const
 // One Taylor term for every sector of a block-diagonal stack (int32 indptr).
 // sec_off: device int64[nsec+1] row offsets; mu: device complex128[nsec];
 // coeff: device complex128 table; ctl: MultiCtl (qs_multi_ctl_bytes()) with
-// nsec set.  dtype QS_F64 / QS_C128 with btype QS_C128, or QS_F32 / QS_C64 /
-// QS_F64 with btype QS_C64.  group as for qs_taylor_term.
+// nsec set.  btype / dtype pairs as for qs_taylor_term.  group as for
+// qs_taylor_term.
 extern "C" int qs_taylor_multi_term(int64_t n, const void *indptr, const int32_t *indices, const void *data, int dtype,
                                     const void *Bin, void *Bout, int btype, void *F, int64_t nvec,
                                     const int64_t *sec_off, const void *mu, const void *coeff, int j, double tol,
@@ -702,13 +599,14 @@ extern "C" int qs_taylor_multi_term(int64_t n, const void *indptr, const int32_t
     const cdbl *m = reinterpret_cast<const cdbl *>(mu);
     const cdbl *cf = reinterpret_cast<const cdbl *>(coeff);
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
+    if (lp_btype(btype)) {
+        LpTerm a{n, indptr, 0, indices, data, dtype, Bin, Bout, btype, Fp, nvec, cdbl{0.0, 0.0}, m, sec_off, cf, j, tol,
+                 ctl, G, U, st};
+        return lp_taylor_term(a, true);
+    }
     if (btype == QS_C128) {
         if (dtype == QS_F64) return multi_nb<double, cdbl>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
         if (dtype == QS_C128) return multi_nb<cdbl, cdbl>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
-    } else if (btype == QS_C64) {
-        if (dtype == QS_F32) return multi_nb<float, cflt>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
-        if (dtype == QS_C64) return multi_nb<cflt, cflt>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
-        if (dtype == QS_F64) return multi_nb<double, cflt>(n, indptr, indices, data, Bin, Bout, Fp, nvec, sec_off, m, cf, j, tol, c, G, U, st);
     }
     return QS_ERR_ARG;
 }
@@ -718,15 +616,13 @@ extern "C" int qs_taylor_multi_rescale(int64_t n, int64_t nvec, void *F, void *B
 {
     if (n < 1 || nvec < 1 || !F || !B0 || !sec_off || !ctl || (use_eta && !eta)) return QS_ERR_ARG;
     cudaStream_t st = qs_stream(stream);
+    if (lp_btype(btype))
+        return lp_taylor_rescale(n, nvec, (cdbl *)F, B0, btype, (const cdbl *)eta, use_eta, sec_off, ctl, 0, true, st);
+    if (btype != QS_C128) return QS_ERR_ARG;
     int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
     int blocks = (int)(b > cap ? cap : b);
-    if (btype == QS_C128)
-        taylor_multi_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, sec_off,
-                                                                 (const cdbl *)eta, use_eta, (MultiCtl *)ctl);
-    else if (btype == QS_C64)
-        taylor_multi_rescale_kernel<cflt><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cflt *)B0, sec_off,
-                                                                 (const cdbl *)eta, use_eta, (MultiCtl *)ctl);
-    else return QS_ERR_ARG;
+    taylor_multi_rescale_kernel<cdbl><<<blocks, 256, 0, st>>>(n, nvec, (cdbl *)F, (cdbl *)B0, sec_off,
+                                                             (const cdbl *)eta, use_eta, (MultiCtl *)ctl);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }

@@ -1,0 +1,437 @@
+// Fused Taylor term without FP64 instructions per nonzero.
+//
+// Same recurrence and stopping test as csrc/expm.cu (scipy's
+// _expm_multiply_simple_core with the shift folded in, which the reference's
+// parallel-sparse-tools==0.2.5 loop follows: expm_multiply_parallel_core.html
+// :347-372), for two storage forms of the Taylor term B:
+//
+//   * QS_CPF  - paired single precision (csrc/pairf.cuh): B and the matrix
+//               values are hi + lo float pairs, products and row sums run in
+//               FP32 instructions with 48-bit significands; the default
+//               "double" form of the Python layer;
+//   * QS_C64  - complex64 B and float32 / complex64 values with FP32 row sums:
+//               the mixed form.
+//
+// In both, the Taylor partial sum F, the trace shift, the coefficients and
+// the stopping test stay in IEEE double.  B is stored scaled by 2^-bexp,
+// where 2^bexp is the power of two at or below ||F||_inf at the start of the
+// substep, so the float exponent range covers any input scale; the scale is
+// undone exactly on the exponent when a term is added to F.
+//
+// Per row the G lanes split the nonzeros; after the butterfly reduction every
+// lane holds the row sum, lanes 0 and 1 write the real and imaginary part of
+// the new term and of F (two FP64 adds each for the paired form), so the
+// FP64 pipe sees a handful of fully used instructions per row instead of
+// two per nonzero.  Row norms for the stopping test are taken in FP32 from
+// the scaled values.
+#include "qs_common.cuh"
+#include "expm_ctl.cuh"
+#include "pairf.cuh"
+#include "lp_modes.cuh"
+
+namespace {
+
+// One Taylor term; MULTI: block-diagonal stack of sectors (MultiCtl), else one
+// matrix (ExpmCtl).  lgG: log2 of the lanes per row.
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
+__global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, const IT *__restrict__ indptr,
+                                                        const int32_t *__restrict__ indices,
+                                                        const DV *__restrict__ data,
+                                                        const typename M::BE *__restrict__ Bin,
+                                                        typename M::BE *__restrict__ Bout, cdbl *__restrict__ F,
+                                                        int64_t nvec, cdbl mu0, const cdbl *__restrict__ mus,
+                                                        const int64_t *__restrict__ sec_off,
+                                                        const cdbl *__restrict__ coeff, int j, double tol, void *ctlp)
+{
+    using S = typename M::S;
+    using BE = typename M::BE;
+    constexpr int NS = MULTI ? QS_MAX_SECTORS : 1;
+    __shared__ S s_mu[2 * NS];
+    __shared__ S s_cf[2];
+    __shared__ int s_bexp[NS];
+    __shared__ int s_done[NS];
+    __shared__ int64_t s_off[NS + 1];
+    __shared__ unsigned int s_mb[NS], s_mf[NS];
+    int nsec = 1;
+    if constexpr (!MULTI) {
+        ExpmCtl *ctl = reinterpret_cast<ExpmCtl *>(ctlp);
+        if (*((volatile int *)&ctl->done)) return;
+        if (threadIdx.x == 0) {
+            s_bexp[0] = *((volatile int *)&ctl->bexp);
+            s_done[0] = 0;
+        }
+        if (threadIdx.x == 1) s_mu[0] = M::from_d(mu0.x);
+        if (threadIdx.x == 2) s_mu[1] = M::from_d(mu0.y);
+    } else {
+        MultiCtl *ctl = reinterpret_cast<MultiCtl *>(ctlp);
+        nsec = ctl->nsec;
+        for (int b = threadIdx.x; b <= nsec; b += blockDim.x) s_off[b] = sec_off[b];
+        for (int b = threadIdx.x; b < nsec; b += blockDim.x) {
+            s_done[b] = *((volatile int *)&ctl->done[b]);
+            s_bexp[b] = ctl->bexp[b];
+            const cdbl m = mus[b];
+            s_mu[2 * b] = M::from_d(m.x);
+            s_mu[2 * b + 1] = M::from_d(m.y);
+            s_mb[b] = 0u;
+            s_mf[b] = 0u;
+        }
+    }
+    if (threadIdx.x == 32) s_cf[0] = M::from_d(coeff[j].x);
+    if (threadIdx.x == 33) s_cf[1] = M::from_d(coeff[j].y);
+    __syncthreads();
+
+    const int G = 1 << lgG;
+    const int GPW = 32 >> lgG;
+    const int lane = threadIdx.x & (G - 1);
+    const int comp = lane & 1;
+    const int gsub = (threadIdx.x & 31) >> lgG;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const cx<S> cf{s_cf[0], s_cf[1]};
+    float mb = 0.f, mf = 0.f;
+    // Rows are handed out per warp (GPW consecutive rows per warp and
+    // iteration), so every lane reaches the full-mask shuffles.
+    for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int64_t r = rb + gsub;
+        int sec = 0;
+        if constexpr (MULTI) sec = r < n ? sector_of(s_off, nsec, r) : 0;
+        const bool valid = r < n && !s_done[sec];
+        const bool writer = valid && lane < 2;
+        const IT k0 = valid ? indptr[r] : (IT)0, k1 = valid ? indptr[r + 1] : (IT)0;
+        const int bexp = s_bexp[sec];
+        const cx<S> mu{s_mu[2 * sec], s_mu[2 * sec + 1]};
+        float rbn = 0.f, rfn = 0.f;
+        BE bo_pre{M::zero(), M::zero()};
+        double f_pre = 0.0;
+        if (NB == 1 && writer) {
+            bo_pre = M::ldB(Bin + r);
+            f_pre = __ldcs(reinterpret_cast<const double *>(F + r) + comp);
+        }
+        for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
+            S ar[NB], ai[NB];
+#pragma unroll
+            for (int b = 0; b < NB; b++) ar[b] = ai[b] = M::zero();
+            for (IT k = k0 + lane; k < k1; k += (IT)(G * U)) {
+                int32_t col[U];
+                DV d[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const IT kk = k + (IT)(u * G);
+                    const bool in = kk < k1;
+                    col[u] = in ? __ldcs(indices + kk) : 0;
+                    d[u] = in ? ldv(data + kk) : vzero<DV>();
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    if (k + (IT)(u * G) < k1) {
+#pragma unroll
+                        for (int b = 0; b < NB; b++)
+                            if (NB == 1 || c0 + b < nvec)
+                                vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(Bin + (int64_t)col[u] * nvec + c0 + b));
+                    }
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                for (int o = G >> 1; o > 0; o >>= 1) {
+                    ar[b] = M::merge(ar[b], M::shfl_xor(ar[b], o));
+                    ai[b] = M::merge(ai[b], M::shfl_xor(ai[b], o));
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                if (c0 + b >= nvec) break;
+                const int64_t e = r * nvec + c0 + b;
+                const BE bo = NB == 1 ? bo_pre : (writer ? M::ldB(Bin + e) : BE{M::zero(), M::zero()});
+                const S accr = M::fin(ar[b]), acci = M::fin(ai[b]);
+                // w = A B - mu B;  new term = cf w
+                const S wr = M::sub(accr, M::sub(M::mul(mu.re, bo.re), M::mul(mu.im, bo.im)));
+                const S wi = M::sub(acci, M::add(M::mul(mu.re, bo.im), M::mul(mu.im, bo.re)));
+                const S bnr = M::sub(M::mul(cf.re, wr), M::mul(cf.im, wi));
+                const S bni = M::add(M::mul(cf.re, wi), M::mul(cf.im, wr));
+                const float nb2 = M::hi(bnr) * M::hi(bnr) + M::hi(bni) * M::hi(bni);
+                float fc = 0.f;
+                if (writer) {
+                    const S mine = comp ? bni : bnr;
+                    M::st_comp(Bout + e, comp, mine);
+                    double *fp = reinterpret_cast<double *>(F + e) + comp;
+                    double fv = NB == 1 ? f_pre : __ldcs(fp);
+                    fv = M::add_to(fv, mine, bexp);
+                    __stcs(fp, fv);
+                    fc = d2f_scaled(fv, bexp);
+                }
+                float f2 = fc * fc;
+                f2 += __shfl_xor_sync(0xffffffffu, f2, 1);
+                if (NB == 1) {
+                    rbn = nb2;          // one column: squared moduli, square root once at the end
+                    rfn = f2;
+                } else {
+                    rbn += sqrtf(nb2);
+                    rfn += sqrtf(f2);
+                }
+            }
+        }
+        if (writer) {
+            if constexpr (MULTI) {
+                if (lane == 0) {
+                    atomicMax(&s_mb[sec], __float_as_uint(rbn));
+                    atomicMax(&s_mf[sec], __float_as_uint(rfn));
+                }
+            } else {
+                mb = fmaxf(mb, rbn);
+                mf = fmaxf(mf, rfn);
+            }
+        }
+    }
+
+    if constexpr (!MULTI) {
+        ExpmCtl *ctl = reinterpret_cast<ExpmCtl *>(ctlp);
+        fold_max2(f2d_scaled(mb, 0), f2d_scaled(mf, 0), &ctl->c2, &ctl->fn);
+        if (last_block(ctl) && threadIdx.x == 0) {
+            volatile ExpmCtl *vc = ctl;
+            double c2 = __longlong_as_double((long long)vc->c2);
+            double fn = __longlong_as_double((long long)vc->fn);
+            if (nvec == 1) { c2 = sqrt(c2); fn = sqrt(fn); }
+            const double sc = pow2(s_bexp[0]);
+            c2 *= sc;
+            fn *= sc;
+            vc->terms = vc->terms + 1;
+            if (vc->c1 + c2 <= tol * fn) vc->done = 1;
+            else vc->c1 = c2;
+            vc->c2 = 0ull;
+            vc->fn = 0ull;
+            __threadfence();
+            vc->arrive = 0u;
+        }
+    } else {
+        MultiCtl *ctl = reinterpret_cast<MultiCtl *>(ctlp);
+        __syncthreads();
+        for (int b = threadIdx.x; b < nsec; b += blockDim.x) {
+            if (s_mb[b]) atomicMax(&ctl->c2[b], (unsigned long long)__double_as_longlong(f2d_scaled(__uint_as_float(s_mb[b]), 0)));
+            if (s_mf[b]) atomicMax(&ctl->fn[b], (unsigned long long)__double_as_longlong(f2d_scaled(__uint_as_float(s_mf[b]), 0)));
+        }
+        if (last_block_multi(ctl) && threadIdx.x == 0) {
+            volatile MultiCtl *vc = ctl;
+            long long active = 0;
+            for (int b = 0; b < nsec; b++) {
+                if (vc->done[b]) continue;
+                active++;
+                double c2 = __longlong_as_double((long long)vc->c2[b]);
+                double fn = __longlong_as_double((long long)vc->fn[b]);
+                if (nvec == 1) { c2 = sqrt(c2); fn = sqrt(fn); }
+                const double sc = pow2(vc->bexp[b]);
+                c2 *= sc;
+                fn *= sc;
+                if (vc->c1[b] + c2 <= tol * fn) vc->done[b] = 1;
+                else vc->c1[b] = c2;
+                vc->c2[b] = 0ull;
+                vc->fn[b] = 0ull;
+            }
+            vc->terms = vc->terms + active;
+            __threadfence();
+            vc->arrive = 0u;
+        }
+    }
+}
+
+// F = eta F (per sector for MULTI) and the row-norm maximum; the last block
+// sets c1 = ||F||_inf, the storage exponent bexp and clears the per-substep
+// state (counting, at a substep end, a stopping test that never fired).
+template <bool MULTI>
+__global__ void __launch_bounds__(256) taylor_lp_norm_kernel(int64_t n, int64_t nvec, cdbl *__restrict__ F,
+                                                             const cdbl *__restrict__ eta, int use_eta,
+                                                             const int64_t *__restrict__ sec_off, void *ctlp,
+                                                             int substep_end)
+{
+    constexpr int NS = MULTI ? QS_MAX_SECTORS : 1;
+    __shared__ int64_t s_off[NS + 1];
+    __shared__ unsigned long long s_m[NS];
+    int nsec = 1;
+    if constexpr (MULTI) {
+        nsec = reinterpret_cast<MultiCtl *>(ctlp)->nsec;
+        for (int b = threadIdx.x; b <= nsec; b += blockDim.x) s_off[b] = sec_off[b];
+        for (int b = threadIdx.x; b < nsec; b += blockDim.x) s_m[b] = 0ull;
+        __syncthreads();
+    }
+    double m = 0.0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int b = 0;
+        if constexpr (MULTI) b = sector_of(s_off, nsec, r);
+        const cdbl et = use_eta ? eta[b] : cdbl{1.0, 0.0};
+        const bool scale = !(et.x == 1.0 && et.y == 0.0);
+        double rs = 0.0;
+        for (int64_t c = 0; c < nvec; c++) {
+            const int64_t e = r * nvec + c;
+            cdbl f = F[e];
+            if (scale) {
+                f = cdbl{et.x * f.x - et.y * f.y, et.x * f.y + et.y * f.x};
+                F[e] = f;
+            }
+            rs += hypot(f.x, f.y);
+        }
+        if constexpr (MULTI) atomicMax(&s_m[b], (unsigned long long)__double_as_longlong(rs));
+        else m = fmax(m, rs);
+    }
+    if constexpr (!MULTI) {
+        ExpmCtl *ctl = reinterpret_cast<ExpmCtl *>(ctlp);
+        fold_max2(m, 0.0, &ctl->c2, nullptr);
+        if (last_block(ctl) && threadIdx.x == 0) {
+            volatile ExpmCtl *vc = ctl;
+            const double c1 = __longlong_as_double((long long)vc->c2);
+            vc->c1 = c1;
+            vc->bexp = scale_exp(c1);
+            vc->c2 = 0ull;
+            vc->fn = 0ull;
+            if (substep_end && !vc->done) vc->nonconv = vc->nonconv + 1;
+            vc->done = 0;
+            __threadfence();
+            vc->arrive = 0u;
+        }
+    } else {
+        MultiCtl *ctl = reinterpret_cast<MultiCtl *>(ctlp);
+        __syncthreads();
+        for (int b = threadIdx.x; b < nsec; b += blockDim.x)
+            if (s_m[b]) atomicMax(&ctl->c2[b], s_m[b]);
+        if (last_block_multi(ctl) && threadIdx.x == 0) {
+            volatile MultiCtl *vc = ctl;
+            for (int b = 0; b < nsec; b++) {
+                const double c1 = __longlong_as_double((long long)vc->c2[b]);
+                vc->c1[b] = c1;
+                vc->bexp[b] = scale_exp(c1);
+                vc->c2[b] = 0ull;
+                vc->fn[b] = 0ull;
+                vc->done[b] = 0;
+            }
+            __threadfence();
+            vc->arrive = 0u;
+        }
+    }
+}
+
+// B0 = F 2^-bexp in the storage form of M
+template <class M, bool MULTI>
+__global__ void __launch_bounds__(256) taylor_lp_load_kernel(int64_t n, int64_t nvec, const cdbl *__restrict__ F,
+                                                             typename M::BE *__restrict__ B0,
+                                                             const int64_t *__restrict__ sec_off, const void *ctlp)
+{
+    constexpr int NS = MULTI ? QS_MAX_SECTORS : 1;
+    __shared__ int64_t s_off[NS + 1];
+    __shared__ double s_sc[NS];
+    int nsec = 1;
+    if constexpr (MULTI) {
+        const MultiCtl *ctl = reinterpret_cast<const MultiCtl *>(ctlp);
+        nsec = ctl->nsec;
+        for (int b = threadIdx.x; b <= nsec; b += blockDim.x) s_off[b] = sec_off[b];
+        for (int b = threadIdx.x; b < nsec; b += blockDim.x) s_sc[b] = pow2(-ctl->bexp[b]);
+    } else {
+        if (threadIdx.x == 0) s_sc[0] = pow2(-reinterpret_cast<const ExpmCtl *>(ctlp)->bexp);
+    }
+    __syncthreads();
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int b = 0;
+        if constexpr (MULTI) b = sector_of(s_off, nsec, r);
+        const double sc = s_sc[b];
+        for (int64_t c = 0; c < nvec; c++) {
+            const int64_t e = r * nvec + c;
+            const cdbl f = F[e];
+            M::st(B0 + e, typename M::BE{M::from_d(f.x * sc), M::from_d(f.y * sc)});
+        }
+    }
+}
+
+__global__ void split_pairs_kernel(int64_t count, const double *__restrict__ src, float2 *__restrict__ dst)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const pf v = pf_from_double(src[i]);
+        dst[i] = make_float2(v.h, v.l);
+    }
+}
+
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
+int lp_go(const LpTerm &a)
+{
+    int lg = 0;
+    while ((1 << lg) < a.G) lg++;
+    const int blocks = taylor_grid(a.n, a.G);
+    taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+        a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
+        (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+template <class M, class DV, class IT, bool MULTI>
+int lp_nb(const LpTerm &a)
+{
+    if (a.nvec == 1) {
+        if constexpr (sizeof(IT) == 4) {
+            if (a.U >= 4 && !MULTI) return lp_go<M, DV, IT, 1, 4, MULTI>(a);
+            if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, MULTI>(a);
+        }
+        return lp_go<M, DV, IT, 1, 1, MULTI>(a);
+    }
+    if (a.nvec == 2) return lp_go<M, DV, IT, 2, 1, MULTI>(a);
+    if (a.nvec <= 4) return lp_go<M, DV, IT, 4, 1, MULTI>(a);
+    return lp_go<M, DV, IT, 8, 1, MULTI>(a);
+}
+
+template <class M, class DV, bool MULTI>
+int lp_idx(const LpTerm &a)
+{
+    if constexpr (!MULTI) {
+        if (a.idx64) return lp_nb<M, DV, int64_t, false>(a);
+    }
+    return lp_nb<M, DV, int32_t, MULTI>(a);
+}
+
+}  // namespace
+
+int lp_taylor_term(const LpTerm &a, bool multi)
+{
+    if (a.G != 2 && a.G != 4 && a.G != 8 && a.G != 16 && a.G != 32) return QS_ERR_ARG;
+    if (multi && a.idx64) return QS_ERR_ARG;
+    if (a.btype == QS_CPF) {
+        if (a.dtype == QS_PF) return multi ? lp_idx<ModePF, pf, true>(a) : lp_idx<ModePF, pf, false>(a);
+        if (a.dtype == QS_CPF) return multi ? lp_idx<ModePF, cpf, true>(a) : lp_idx<ModePF, cpf, false>(a);
+    } else if (a.btype == QS_C64) {
+        if (a.dtype == QS_F32) return multi ? lp_idx<ModeF32, float, true>(a) : lp_idx<ModeF32, float, false>(a);
+        if (a.dtype == QS_C64)
+            return multi ? lp_idx<ModeF32, cx<float>, true>(a) : lp_idx<ModeF32, cx<float>, false>(a);
+    }
+    return QS_ERR_ARG;
+}
+
+int lp_taylor_rescale(int64_t n, int64_t nvec, cdbl *F, void *B0, int btype, const cdbl *eta, int use_eta,
+                      const int64_t *sec_off, void *ctl, int substep_end, bool multi, cudaStream_t st)
+{
+    if (!lp_btype(btype)) return QS_ERR_ARG;
+    int64_t b = (n + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
+    const int blocks = (int)(b > cap ? cap : b);
+    if (multi) taylor_lp_norm_kernel<true><<<blocks, 256, 0, st>>>(n, nvec, F, eta, use_eta, sec_off, ctl, substep_end);
+    else taylor_lp_norm_kernel<false><<<blocks, 256, 0, st>>>(n, nvec, F, eta, use_eta, sec_off, ctl, substep_end);
+    QS_CHECK(cudaGetLastError());
+    if (btype == QS_CPF) {
+        if (multi) taylor_lp_load_kernel<ModePF, true><<<blocks, 256, 0, st>>>(n, nvec, F, (cpf *)B0, sec_off, ctl);
+        else taylor_lp_load_kernel<ModePF, false><<<blocks, 256, 0, st>>>(n, nvec, F, (cpf *)B0, sec_off, ctl);
+    } else {
+        if (multi)
+            taylor_lp_load_kernel<ModeF32, true><<<blocks, 256, 0, st>>>(n, nvec, F, (cx<float> *)B0, sec_off, ctl);
+        else
+            taylor_lp_load_kernel<ModeF32, false><<<blocks, 256, 0, st>>>(n, nvec, F, (cx<float> *)B0, sec_off, ctl);
+    }
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+// dst[i] = (hi, lo) with hi = float(src[i]), lo = float(src[i] - hi): the
+// paired form of a double array (a complex128 array splits into the
+// {re.hi, re.lo, im.hi, im.lo} layout of QS_CPF).
+extern "C" int qs_split_pairs(int64_t count, const double *src, void *dst, void *stream)
+{
+    if (count < 0 || (count > 0 && (!src || !dst))) return QS_ERR_ARG;
+    if (count == 0) return QS_OK;
+    int64_t b = (count + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
+    split_pairs_kernel<<<(int)(b > cap ? cap : b), 256, 0, qs_stream(stream)>>>(count, src, (float2 *)dst);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}

@@ -1,0 +1,130 @@
+// Arithmetic policies of the float-instruction sparse kernels
+// (csrc/expm_lp.cu, csrc/spmv_lp.cu): ModePF keeps values as float pairs
+// (csrc/pairf.cuh), ModeF32 as plain floats.  Each gives the scalar type S,
+// the complex element BE of the gathered vector, the product-accumulate and
+// the butterfly merge of partial row sums, small complex arithmetic for the
+// row epilogue and the conversions to IEEE double.
+#pragma once
+#include "qs_common.cuh"
+#include "pairf.cuh"
+
+namespace {
+
+struct ModePF {
+    using S = pf;
+    using BE = cpf;
+    __device__ static S zero() { return pf{0.f, 0.f}; }
+    __device__ static BE ldB(const BE *p)
+    {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+        return BE{pf{v.x, v.y}, pf{v.z, v.w}};
+    }
+    __device__ static void fma(S &acc, S a, S b) { pf_fma(acc, a.h, a.l, b.h, b.l); }
+    __device__ static S merge(S a, S b) { return pf_merge(a, b); }
+    __device__ static S fin(S a) { return pf_norm(a); }
+    __device__ static S add(S a, S b) { return pf_add(a, b); }
+    __device__ static S sub(S a, S b) { return pf_sub(a, b); }
+    __device__ static S mul(S a, S b) { return pf_mul(a, b); }
+    __device__ static S neg(S a) { return pf_neg(a); }
+    __device__ static float hi(S a) { return a.h; }
+    __device__ static S from_d(double x) { return pf_from_double(x); }
+    __device__ static S shfl_xor(S a, int o)
+    {
+        return pf{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+    }
+    __device__ static S ldS(const S *p)
+    {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return pf{v.x, v.y};
+    }
+    __device__ static double add_to(double f, S v, int k) { return (f + f2d_scaled(v.h, k)) + f2d_scaled(v.l, k); }
+    __device__ static double to_d(S v, int k) { return f2d_scaled(v.h, k) + f2d_scaled(v.l, k); }
+    __device__ static void st_comp(BE *p, int comp, S v)
+    {
+        __stcs(reinterpret_cast<float2 *>(p) + comp, make_float2(v.h, v.l));
+    }
+    __device__ static void st(BE *p, BE v)
+    {
+        __stcs(reinterpret_cast<float4 *>(p), make_float4(v.re.h, v.re.l, v.im.h, v.im.l));
+    }
+};
+
+struct ModeF32 {
+    using S = float;
+    using BE = cx<float>;
+    __device__ static S zero() { return 0.f; }
+    __device__ static BE ldB(const BE *p)
+    {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return BE{v.x, v.y};
+    }
+    __device__ static void fma(S &acc, S a, S b) { acc = __fmaf_rn(a, b, acc); }
+    __device__ static S merge(S a, S b) { return a + b; }
+    __device__ static S fin(S a) { return a; }
+    __device__ static S add(S a, S b) { return a + b; }
+    __device__ static S sub(S a, S b) { return a - b; }
+    __device__ static S mul(S a, S b) { return a * b; }
+    __device__ static S neg(S a) { return -a; }
+    __device__ static float hi(S a) { return a; }
+    __device__ static S from_d(double x) { return (float)x; }
+    __device__ static S shfl_xor(S a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+    __device__ static S ldS(const S *p) { return __ldg(p); }
+    __device__ static double add_to(double f, S v, int k) { return f + f2d_scaled(v, k); }
+    __device__ static double to_d(S v, int k) { return f2d_scaled(v, k); }
+    __device__ static void st_comp(BE *p, int comp, S v) { __stcs(reinterpret_cast<float *>(p) + comp, v); }
+    __device__ static void st(BE *p, BE v) { __stcs(reinterpret_cast<float2 *>(p), make_float2(v.re, v.im)); }
+};
+
+// streamed loads of the matrix values
+__device__ __forceinline__ pf ldv(const pf *p)
+{
+    const float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    return pf{v.x, v.y};
+}
+__device__ __forceinline__ cpf ldv(const cpf *p)
+{
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(p));
+    return cpf{pf{v.x, v.y}, pf{v.z, v.w}};
+}
+__device__ __forceinline__ float ldv(const float *p) { return __ldcs(p); }
+__device__ __forceinline__ cx<float> ldv(const cx<float> *p)
+{
+    const float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    return cx<float>{v.x, v.y};
+}
+template <class DV> __device__ __forceinline__ DV vzero() { return DV{}; }
+
+// acc += d x for a real value d and a complex x
+template <class M>
+__device__ __forceinline__ void vmul_acc(typename M::S &ar, typename M::S &ai, typename M::S d,
+                                         const typename M::BE &x)
+{
+    M::fma(ar, d, x.re);
+    M::fma(ai, d, x.im);
+}
+// acc += d x for a complex value d
+template <class M>
+__device__ __forceinline__ void vmul_acc(typename M::S &ar, typename M::S &ai, const cx<typename M::S> &d,
+                                         const typename M::BE &x)
+{
+    M::fma(ar, d.re, x.re);
+    M::fma(ar, M::neg(d.im), x.im);
+    M::fma(ai, d.re, x.im);
+    M::fma(ai, d.im, x.re);
+}
+
+// exponent of the largest power of two <= x (0 for 0, subnormal or non-finite x)
+__device__ __forceinline__ int scale_exp(double x)
+{
+    const int E = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffull);
+    if (E == 0 || E == 0x7ff) return 0;
+    int k = E - 1023;
+    return k < -1000 ? -1000 : (k > 1000 ? 1000 : k);
+}
+
+__device__ __forceinline__ double pow2(int k)   // 2^k for |k| <= 1000
+{
+    return __hiloint2double((1023 + k) << 20, 0);
+}
+
+}  // namespace

@@ -17,6 +17,8 @@
 #define QS_F64 1
 #define QS_C64 2
 #define QS_C128 3
+#define QS_PF 4        // real value kept as a pair of floats hi + lo (8 bytes)
+#define QS_CPF 5       // complex value kept as two float pairs {re.hi, re.lo, im.hi, im.lo} (16 bytes)
 
 #define QS_CHECK(call)                                   \
     do {                                                 \

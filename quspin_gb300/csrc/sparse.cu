@@ -9,7 +9,11 @@
 // and the numpy BLAS-1 steps of the Lanczos recurrence
 // (src/quspin/tools/lanczos/_lanczos_utils.py:186-204).
 //
-// CSR SpMV: a group of G lanes (4..32, a power of two) owns one row, reads the
+// The kernels here compute in IEEE double; csrc/spmv_lp.cu holds the
+// paired-single form for float64 / complex128 vectors (qs_csr_matvec_pairs)
+// and the FP32 form that qs_csr_matvec uses for float32 / complex64 vectors.
+//
+// CSR SpMV: a group of G lanes (2..32, a power of two) owns one row, reads the
 // row's values and column indices with coalesced loads, gathers x through L2
 // and reduces with warp shuffles.  For k right-hand sides (C order [n, k]) each
 // lane keeps NB complex accumulators per row and x rows are read as
@@ -226,6 +230,10 @@ static int spmm_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // precision never exceeds the vector precision's partner).  group: launch
 // shape, G | (U << 8) with G lanes per row (2..32) and U in-flight entries per
 // lane (1, 2, 4); 0 picks G from nnz/n and U = 2.
+int spmv_lp_single(int64_t n, const void *indptr, int idx64, const int32_t *indices, const void *data, int dtype,
+                   const void *x, int xtype, void *y, int64_t nvec, cdbl a, int overwrite, int G, int U,
+                   cudaStream_t st);
+
 extern "C" int qs_csr_matvec(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                              const void *data, int dtype, const void *x, int xtype, void *y, int64_t nvec,
                              double a_re, double a_im, int overwrite, int group, void *stream)
@@ -247,7 +255,8 @@ extern "C" int qs_csr_matvec(int64_t n, int64_t nnz, const void *indptr, int idx
         if (dtype == QS_F32) return spmm_idx<float, double>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     case QS_F32:
-        if (dtype == QS_F32) return spmm_idx<float, float>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_F32)   // FP32 products and row sums (csrc/spmv_lp.cu)
+            return spmv_lp_single(n, indptr, idx64, indices, data, dtype, x, xtype, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     case QS_C128:
         if (dtype == QS_F64) return spmm_idx<double, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
@@ -256,8 +265,8 @@ extern "C" int qs_csr_matvec(int64_t n, int64_t nnz, const void *indptr, int idx
         if (dtype == QS_C64) return spmm_idx<cflt, cdbl>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     case QS_C64:
-        if (dtype == QS_F32) return spmm_idx<float, cflt>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
-        if (dtype == QS_C64) return spmm_idx<cflt, cflt>(idx64, n, indptr, indices, data, x, y, nvec, a, overwrite, G, U, st);
+        if (dtype == QS_F32 || dtype == QS_C64)
+            return spmv_lp_single(n, indptr, idx64, indices, data, dtype, x, xtype, y, nvec, a, overwrite, G, U, st);
         return QS_ERR_ARG;
     default:
         return QS_ERR_ARG;

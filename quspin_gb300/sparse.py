@@ -18,6 +18,23 @@ from . import _device as D
 from . import _lib
 
 
+# Arithmetic of the CSR product for float64 / complex128 vectors: "double"
+# (values and x as float pairs, FP32-instruction products with 48-bit
+# significands, csrc/spmv_lp.cu; GB300's FP64 pipe is a small fraction of its
+# FP32 rate) or "ieee" (IEEE double products, csrc/sparse.cu).  float32 /
+# complex64 vectors always use FP32 products.
+SPMV_PRECISION = "double"
+
+
+def set_spmv_precision(precision):
+    """Module default for DeviceCSR.matvec_into; returns the previous one."""
+    global SPMV_PRECISION
+    if precision not in ("double", "ieee"):
+        raise ValueError("precision must be 'double' or 'ieee'")
+    old, SPMV_PRECISION = SPMV_PRECISION, precision
+    return old
+
+
 def result_dtype(*dtypes):
     return np.result_type(*[np.dtype(d) for d in dtypes])
 
@@ -39,6 +56,19 @@ class DeviceCSR:
         if self._nnz is None:
             self._nnz = int(self.indptr[-1].item()) if self.shape[0] > 0 else 0
         return self._nnz
+
+    @property
+    def vcode(self):
+        """Element type code of the values for the C ABI."""
+        return D.code(self.dtype)
+
+    def paired(self):
+        """The values split into float pairs (``PairedCSR``), cached."""
+        p = self.__dict__.get("_paired")
+        if p is None:
+            p = PairedCSR(self)
+            self._paired = p
+        return p
 
     @classmethod
     def from_scipy(cls, A, dtype=None):
@@ -67,16 +97,38 @@ class DeviceCSR:
             return self
         return DeviceCSR(self.indptr, self.indices, self.data.to(D.torch_dtype(dtype)), self.shape, dtype)
 
-    def matvec_into(self, x, y, a=1.0, overwrite=True, group=None):
+    def _pair_scratch(self, count):
+        """Device scratch for x split into float pairs (count doubles) and
+        its norm word."""
+        sc = self.__dict__.get("_xs")
+        if sc is None or sc[0].numel() < 2 * count:
+            sc = (torch.empty(max(2 * count, 2), dtype=torch.float32, device=D.device()),
+                  torch.zeros(1, dtype=torch.int64, device=D.device()))
+            self._xs = sc
+        return sc
+
+    def matvec_into(self, x, y, a=1.0, overwrite=True, group=None, precision=None):
         """y (=|+=) a * A x on device tensors of the result dtype.  group:
-        launch shape code (None: the autotuned one for this matrix)."""
+        launch shape code (None: the autotuned one for this matrix);
+        precision: "double" / "ieee" for float64 / complex128 vectors (None:
+        the module default)."""
         n = self.shape[0]
         nvec = 1 if x.dim() == 1 else x.shape[1]
         xt = D.np_dtype(x.dtype)
+        prec = SPMV_PRECISION if precision is None else precision
+        paired = (prec == "double" and xt in (np.dtype(np.float64), np.dtype(np.complex128))
+                  and not (self.dtype.kind == "c" and xt.kind != "c"))
         if group is None:
             from .tune import tune_spmv
-            group = tune_spmv(self, nvec, xt)
+            group = tune_spmv(self, nvec, xt, prec)
         a = complex(a)
+        if paired:
+            P = self.paired()
+            xs, nrm = self._pair_scratch(x.numel() * (2 if xt.kind == "c" else 1))
+            _lib.call("qs_csr_matvec_pairs", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
+                      D.ptr(P.data), P.vcode, D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,
+                      int(bool(overwrite)), int(group), D.ptr(xs), D.ptr(nrm), D.stream())
+            return y
         _lib.call("qs_csr_matvec", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
                   D.ptr(self.data), D.code(self.dtype), D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,
                   int(bool(overwrite)), int(group), D.stream())
@@ -191,6 +243,37 @@ class DeviceDIA:
 
     def trace(self):
         return self.tocsr().diagonal().sum()
+
+
+class PairedCSR:
+    """A DeviceCSR whose values are kept as float pairs hi + lo (type codes
+    PF / CPF), the operand form of the paired-single Taylor kernels
+    (csrc/expm_lp.cu).  Shares indptr and indices with its source."""
+
+    format = "csr"
+
+    def __init__(self, M):
+        self.indptr, self.indices, self.shape, self.idx64 = M.indptr, M.indices, M.shape, M.idx64
+        self._nnz = M.nnz
+        self.complex = M.dtype.kind == "c"
+        self.dtype = np.dtype(np.complex128 if self.complex else np.float64)
+        src = M.data.to(D.torch_dtype(self.dtype)).contiguous()
+        count = src.numel() * (2 if self.complex else 1)
+        self.data = torch.empty(max(2 * count, 2), dtype=torch.float32, device=D.device())
+        _lib.call("qs_split_pairs", count, D.ptr(src), D.ptr(self.data), D.stream())
+
+    @property
+    def nnz(self):
+        return self._nnz
+
+    @property
+    def vcode(self):
+        return _lib.CPF if self.complex else _lib.PF
+
+    def refresh(self, data):
+        """Re-split new values (same pattern) into the pair buffer."""
+        count = data.numel() * (2 if self.complex else 1)
+        _lib.call("qs_split_pairs", count, D.ptr(data), D.ptr(self.data), D.stream())
 
 
 def to_device_matrix(A, dtype=None):

@@ -32,7 +32,9 @@ def _parallel_cols(S, T, n):
     (entries are unit modulus, so parallel means |<s, t>| == n)."""
     if T is None or T.shape[1] == 0:
         return torch.zeros(S.shape[1], dtype=torch.bool, device=S.device)
-    G = (S.conj().T @ T).abs()
+    # inner products as broadcast products and column sums (a [1, n] x [n, m]
+    # library GEMM with a long inner dimension is far slower on the device)
+    G = (S.conj().unsqueeze(2) * T.unsqueeze(1)).sum(dim=0).abs()
     return (G >= n - 0.5).any(dim=1)
 
 

@@ -13,9 +13,11 @@ The schedule is common to all sectors: s = max_b s_b substeps of at most
 m* = max_b m*_b terms, each sector's (m*_b, s_b) chosen as
 ``ExpmMultiplyParallel`` does; more substeps than a sector needs only
 tightens its truncation, and each sector still stops on its own test.
-``precision="mixed"`` stores the matrix values in float32/complex64 and the
-Taylor term blocks in complex64, keeping F, shifts, coefficients and norms
-in double precision.  The launch shape is autotuned on the stacked matrix.
+``precision`` is as for ``ExpmMultiplyParallel``: "double" (float-pair
+products, the default), "ieee" (IEEE double products) or "mixed" (complex64
+term blocks and float32/complex64 values); F, shifts, coefficients and the
+stopping tests stay in double precision.  The launch shape is autotuned on
+the stacked matrix.
 """
 from __future__ import annotations
 
@@ -56,8 +58,8 @@ class MultiSectorExpm:
     """e^{a H_b} V_b for every sector b in one graph-captured launch sequence."""
 
     def __init__(self, matrices, a, nvec=1, precision="double", graph=True):
-        if precision not in ("double", "mixed"):
-            raise ValueError("precision must be 'double' or 'mixed'")
+        if precision not in ("double", "ieee", "mixed"):
+            raise ValueError("precision must be 'double', 'ieee' or 'mixed'")
         if len(matrices) > _lib.load().qs_max_sectors():
             raise ValueError("at most {} sectors per launch".format(_lib.load().qs_max_sectors()))
         self._a = complex(a)
@@ -77,14 +79,17 @@ class MultiSectorExpm:
         if precision == "mixed":
             A = A.astype(np.float32 if A.dtype.kind == "f" else np.complex64)
             self._btype = _lib.C64
-        else:
+        elif precision == "ieee":
             self._btype = _lib.C128
+        else:
+            A = A.paired()
+            self._btype = _lib.CPF
         self._A = A
         n, k = A.shape[0], self.nvec
         self.n = n
         dev = D.device()
         self.F = torch.zeros((n, k), dtype=torch.complex128, device=dev)
-        bdt = torch.complex128 if self._btype == _lib.C128 else torch.complex64
+        bdt = torch.complex64 if self._btype == _lib.C64 else torch.complex128
         self._work = torch.empty(2 * n * k, dtype=bdt, device=dev)
         self._soff = torch.tensor(offs, dtype=torch.int64, device=dev)
         mus = np.array([complex(p._mu) for p in self._plain], np.complex128)
@@ -108,7 +113,7 @@ class MultiSectorExpm:
 
     def _term(self, j, bin_, bout, tol, group):
         A = self._A
-        _lib.call("qs_taylor_multi_term", self.n, D.ptr(A.indptr), D.ptr(A.indices), D.ptr(A.data), D.code(A.dtype),
+        _lib.call("qs_taylor_multi_term", self.n, D.ptr(A.indptr), D.ptr(A.indices), D.ptr(A.data), A.vcode,
                   D.ptr(bin_), D.ptr(bout), self._btype, D.ptr(self.F), self.nvec, D.ptr(self._soff),
                   D.ptr(self._mu), D.ptr(self._coeff), j, tol, D.ptr(self._ctl), group, D.stream())
 

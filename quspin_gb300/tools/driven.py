@@ -16,7 +16,9 @@ it, mu(t) from the precomputed per-part traces, and then either
   stopping test firing is counted on the device; such a segment is re-run
   with the plain selection (the fallback).
 
-Many states evolve together as one [n, k] block.
+Many states evolve together as one [n, k] block.  ``precision`` selects the
+Taylor-term arithmetic as for ``ExpmMultiplyParallel`` ("double": float-pair
+products, "ieee": IEEE double products, "mixed": complex64 terms).
 """
 from __future__ import annotations
 
@@ -31,10 +33,13 @@ from ._partition import LazyOperatorNormInfo, fragment_3_1
 
 
 class DrivenEvolution:
-    def __init__(self, H, nvec=1, dtype=np.complex128):
+    def __init__(self, H, nvec=1, dtype=np.complex128, precision="double"):
         from ..operators import hamiltonian
         if not isinstance(H, hamiltonian):
             raise TypeError("H must be a hamiltonian")
+        if precision not in ("double", "ieee", "mixed"):
+            raise ValueError("precision must be 'double', 'ieee' or 'mixed'")
+        self.precision = precision
         self.H = H
         self.nvec = int(nvec)
         parts = [H.static.tocsr()] + [Hd.tocsr() for Hd in H.dynamic.values()]
@@ -65,6 +70,7 @@ class DrivenEvolution:
         self._data = torch.empty_like(self._vals[0])
         self._work = torch.empty(2 * self.n * self.nvec, dtype=torch.complex128, device=D.device())
         self._ctl = torch.zeros(8, dtype=torch.int64, device=D.device())
+        self._op = None
         self.fallbacks = 0
         self.norm_passes = 0
 
@@ -108,14 +114,35 @@ class DrivenEvolution:
                                     device=(torch.complex128, D.device()))
         return fragment_3_1(info, 1, tol, ell=2)
 
+    def _operand(self, M):
+        """M's values (formed on the device for this step) in the operand
+        form of the precision, with the B storage code and launch shape."""
+        from ..tune import tune_taylor
+        if self.precision == "ieee":
+            op, bt = M, _lib.C128
+        elif self.precision == "mixed":
+            vt = torch.float32 if M.dtype.kind == "f" else torch.complex64
+            if self._op is None:
+                self._op = DeviceCSR(M.indptr, M.indices, M.data.to(vt), M.shape, D.np_dtype(vt))
+            self._op.data.copy_(M.data)
+            op, bt = self._op, _lib.C64
+        else:
+            if self._op is None:
+                self._op = M.paired()
+            else:
+                self._op.refresh(M.data)
+            op, bt = self._op, _lib.CPF
+        return op, bt, tune_taylor(op, self.nvec, bt)
+
     def _taylor(self, F, M, mu, a, m, s):
         coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], np.complex128)
         consts = D.to_device(np.concatenate([coeff, [np.exp(a * mu / s), 1.0]]).astype(np.complex128))
         k = max(m, 1)
-        _lib.call("qs_expm_multiply", self.n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
-                  D.code(M.dtype), D.ptr(F), self.nvec, int(s), int(m), float(np.finfo(np.float64).eps / 2),
+        op, bt, group = self._operand(M)
+        _lib.call("qs_expm_multiply", self.n, op.nnz, D.ptr(op.indptr), op.idx64, D.ptr(op.indices), D.ptr(op.data),
+                  op.vcode, D.ptr(F), self.nvec, int(s), int(m), float(np.finfo(np.float64).eps / 2),
                   mu.real, mu.imag, D.ptr(consts[:k]), D.ptr(consts[k:k + 1]), D.ptr(consts[k + 1:]),
-                  D.ptr(self._work), _lib.C128, D.ptr(self._ctl), 0, D.stream())
+                  D.ptr(self._work), bt, D.ptr(self._ctl), group, D.stream())
         self._keep = consts
 
     def run(self, F, t0, dt, nsteps, mode="plain", predictor=None, segment=50, record=None):

@@ -7,13 +7,20 @@ expm_multiply_parallel_core.html:115-463).  Same constructor, ``set_a``,
 ``dot`` and properties; the same dtype rule, tolerance (eps(dtype)/2),
 shift mu = tr(A)/n, exact 1-norm of A - mu I and (m*, s) selection.  The
 trace, 1-norm and every Taylor term run in ``csrc/sparse.cu`` /
-``csrc/expm.cu``; one ``dot`` issues s (m* + 1) + 1 launches and never
-synchronises with the host until the result is read.
+``csrc/expm.cu`` / ``csrc/expm_lp.cu``; one ``dot`` issues about s (m* + 2)
+launches and never synchronises with the host until the result is read.
 
-``precision="mixed"`` is this package's complex64 form: A's values are
-stored in float32 / complex64 and the Taylor term vectors B in complex64
-(half the bytes per term) while F, mu, the coefficients and both norms of the
-stopping test stay in double precision.
+``precision`` chooses the arithmetic of the Taylor terms; the partial sum F,
+mu, the coefficients and the stopping test are IEEE double in all three:
+
+* ``"double"`` (default): A's values and the term vectors B are float pairs
+  hi + lo (48-bit significands) and every per-nonzero product runs in FP32
+  instructions (csrc/pairf.cuh).  GB300's FP64 pipe is a small fraction of
+  its FP32 rate, so this is the fast form of the double-precision method;
+  its state error against IEEE double is of order 1e-14.
+* ``"ieee"``: every product in IEEE double (the reference's arithmetic).
+* ``"mixed"``: complex64 B and float32 / complex64 values with FP32 row
+  sums (half the bytes per term); state error of order 1e-7.
 """
 from __future__ import annotations
 
@@ -54,8 +61,8 @@ class ExpmMultiplyParallel:
         if copy:
             self._Ad = DeviceCSR(self._Ad.indptr.clone(), self._Ad.indices.clone(), self._Ad.data.clone(),
                                  self._Ad.shape, self._Ad.dtype)
-        if precision not in ("double", "mixed"):
-            raise ValueError("precision must be 'double' or 'mixed'")
+        if precision not in ("double", "ieee", "mixed"):
+            raise ValueError("precision must be 'double', 'ieee' or 'mixed'")
         self._precision = precision
         Adt = self._Ad.dtype
         a_dtype_min = np.min_scalar_type(self._a)
@@ -79,6 +86,16 @@ class ExpmMultiplyParallel:
     @property
     def a(self):
         return self._a
+
+    @property
+    def precision(self):
+        return self._precision
+
+    @precision.setter
+    def precision(self, p):
+        if p not in ("double", "ieee", "mixed"):
+            raise ValueError("precision must be 'double', 'ieee' or 'mixed'")
+        self._precision = p
 
     @property
     def A(self):
@@ -158,11 +175,19 @@ class ExpmMultiplyParallel:
             self._mixed = A.astype(vt)
         return self._mixed
 
+    def _operand(self):
+        """(matrix in the value form of the precision, B storage code)."""
+        if self._precision == "mixed":
+            return self._mixed_matrix(), _lib.C64
+        if self._precision == "ieee":
+            return self._Ad, _lib.C128
+        return self._Ad.paired(), _lib.CPF
+
     def _buffers(self, n, nvec, btype):
         key = (n, nvec, btype)
         b = self._bufs.get(key)
         if b is None:
-            esz_dt = torch.complex128 if btype == _lib.C128 else torch.complex64
+            esz_dt = torch.complex64 if btype == _lib.C64 else torch.complex128
             work = torch.empty(2 * n * nvec, dtype=esz_dt, device=D.device())
             ctl = torch.zeros(max(_lib.load().qs_expm_ctl_bytes() // 8, 1) + 1, dtype=torch.int64,
                               device=D.device())
@@ -179,12 +204,10 @@ class ExpmMultiplyParallel:
         a = complex(self._a)
         mu = complex(self._mu)
         s, m = int(self._s), int(self._m_star)
-        mixed = self._precision == "mixed"
-        M = self._mixed_matrix() if mixed else self._Ad
-        btype = _lib.C64 if mixed else _lib.C128
+        M, btype = self._operand()
         wbuf, ctl = self._buffers(n, nvec, btype)
-        if work is not None and not mixed:
-            wbuf = work
+        if work is not None and btype != _lib.C64:
+            wbuf = work          # 16-byte elements: the caller's complex128 work array holds both B buffers
         ctl.zero_()
         coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], dtype=np.complex128)
         eta = np.exp(a * mu / s)
@@ -195,7 +218,7 @@ class ExpmMultiplyParallel:
         from ..tune import tune_taylor
         group = tune_taylor(M, nvec, btype)
         _lib.call("qs_expm_multiply", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
-                  D.code(M.dtype), D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, D.ptr(cf), D.ptr(etap),
+                  M.vcode, D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, D.ptr(cf), D.ptr(etap),
                   D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), group, D.stream())
         self._last_ctl = ctl
         self._consts = consts     # keep alive until the stream reaches it

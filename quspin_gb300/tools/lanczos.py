@@ -26,21 +26,26 @@ __all__ = ["lanczos_full", "lanczos_iter", "lin_comb_Q_T", "expm_lanczos"]
 
 class _DeviceOp:
     """Uniform device product y = A x for the operators this package knows.
-    precision="mixed" applies float32 / complex64 matrix values to the FP64
-    vectors (the recurrence itself stays FP64)."""
+    precision="mixed" runs the product in single precision: x is rounded to
+    float32 / complex64, multiplied by float32 / complex64 matrix values with
+    FP32 row sums, and the result widened back into the FP64 vector y (the
+    recurrence itself stays FP64)."""
 
     def __init__(self, A, precision="double"):
         from ..operators import hamiltonian, quantum_LinearOperator
+        self._x32 = self._y32 = None
         if precision == "mixed":
             if isinstance(A, hamiltonian):
                 A = A.tocsr_gpu()
             if isinstance(A, (DeviceCSR, DeviceDIA)):
                 dt = np.dtype(A.dtype)
-                A0 = A
                 A = A.astype(np.float32 if dt.kind == "f" else np.complex64)
                 self.dtype = dt
             else:
                 raise TypeError("precision='mixed' needs a hamiltonian or a device matrix")
+            self.A = A
+            self._f = self._single
+            return
         self.A = A
         if isinstance(A, (DeviceCSR, DeviceDIA)):
             self._f = lambda x, y: A.matvec_into(x, y, overwrite=True)
@@ -55,8 +60,16 @@ class _DeviceOp:
             self._f = lambda x, y: M.matvec_into(x, y, overwrite=True)
         else:
             raise TypeError("A must be a hamiltonian, quantum_LinearOperator or (sparse) matrix")
-        if precision != "mixed":
-            self.dtype = np.dtype(A.dtype)
+        self.dtype = np.dtype(A.dtype)
+
+    def _single(self, x, y):
+        st = torch.complex64 if x.is_complex() else torch.float32
+        if self._x32 is None or self._x32.shape != x.shape or self._x32.dtype != st:
+            self._x32 = torch.empty(x.shape, dtype=st, device=x.device)
+            self._y32 = torch.empty(x.shape, dtype=st, device=x.device)
+        self._x32.copy_(x)
+        self.A.matvec_into(self._x32, self._y32, overwrite=True)
+        y.copy_(self._y32)
 
     def __call__(self, x, y):
         self._f(x, y)

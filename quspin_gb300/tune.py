@@ -45,9 +45,9 @@ def _time(fn, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
-def tune_spmv(M, nvec=1, xdtype=np.complex128):
+def tune_spmv(M, nvec=1, xdtype=np.complex128, precision="double"):
     """Fastest launch code for M.matvec_into with nvec columns of xdtype."""
-    key = ("spmv", nvec, np.dtype(xdtype).str)
+    key = ("spmv", nvec, np.dtype(xdtype).str, precision)
     cache = M.__dict__.setdefault("_tuned", {})
     if key in cache:
         return cache[key]
@@ -61,7 +61,7 @@ def tune_spmv(M, nvec=1, xdtype=np.complex128):
     best, best_t = 0, None
     for G, U in _candidates(n, M.nnz, nvec):
         code = encode(G, U)
-        t = _time(lambda: M.matvec_into(x, y, group=code))
+        t = _time(lambda: M.matvec_into(x, y, group=code, precision=precision))
         if best_t is None or t < best_t:
             best, best_t = code, t
     cache[key] = best
@@ -78,7 +78,7 @@ def tune_taylor(M, nvec, btype):
     if n < MIN_ROWS or getattr(M, "idx64", 0):
         cache[key] = 0
         return 0
-    bdt = torch.complex128 if btype == _lib.C128 else torch.complex64
+    bdt = torch.complex64 if btype == _lib.C64 else torch.complex128
     b0 = torch.ones(n * nvec, dtype=bdt, device=D.device())
     b1 = torch.empty_like(b0)
     F = torch.zeros(n * nvec, dtype=torch.complex128, device=D.device())
@@ -90,7 +90,7 @@ def tune_taylor(M, nvec, btype):
 
         def run():
             _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
-                      D.code(M.dtype), D.ptr(b0), D.ptr(b1), btype, D.ptr(F), nvec, 0.0, 0.0, D.ptr(coeff), 0, 0.0,
+                      M.vcode, D.ptr(b0), D.ptr(b1), btype, D.ptr(F), nvec, 0.0, 0.0, D.ptr(coeff), 0, 0.0,
                       D.ptr(ctl), code, D.stream())
         t = _time(run)
         if best_t is None or t < best_t:

@@ -60,4 +60,5 @@ def test_multi_sector_mixed_precision(cuda):
     w32 = MultiSectorExpm(mats, a=-2j, nvec=2, precision="mixed").evolve(blocks)
     num = np.sqrt(sum(np.linalg.norm(a - b) ** 2 for a, b in zip(w32, w64)))
     den = np.sqrt(sum(np.linalg.norm(b) ** 2 for b in w64))
-    assert num / den < 1e-6
+    # complex64 terms with FP32 products and row sums: stated tolerance 5e-6
+    assert num / den < 5e-6

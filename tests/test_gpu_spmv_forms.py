@@ -1,0 +1,106 @@
+"""The CSR product in its three arithmetic forms against scipy: float-pair
+products for float64 / complex128 vectors (the default), IEEE double
+products, and FP32 products for float32 / complex64 vectors; the _matvec
+contract (y = a A x or y += a A x, matvec_core.html:146-201) for real and
+complex matrices, one or several right-hand sides and extreme input scales."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+pytestmark = pytest.mark.gpu
+
+
+def _mat(n, cplx, seed):
+    rng = np.random.default_rng(seed)
+    nnz = 30 * n
+    r, c = rng.integers(0, n, nnz), rng.integers(0, n, nnz)
+    v = rng.normal(size=nnz) + (1j * rng.normal(size=nnz) if cplx else 0)
+    return sp.csr_matrix((v, (r, c)), shape=(n, n))
+
+
+def _rel(x, y):
+    return np.linalg.norm(x - y) / np.linalg.norm(y)
+
+
+@pytest.mark.parametrize("cplx_A", [False, True])
+@pytest.mark.parametrize("cplx_x", [False, True])
+@pytest.mark.parametrize("k", [None, 3, 8])
+def test_pair_and_ieee_forms(cuda, cplx_A, cplx_x, k):
+    import torch
+    from quspin_gb300 import _device as D
+    from quspin_gb300.sparse import DeviceCSR
+    n = 70000
+    A = _mat(n, cplx_A, 1)
+    M = DeviceCSR.from_scipy(A)
+    rng = np.random.default_rng(2)
+    shape = (n,) if k is None else (n, k)
+    x = rng.normal(size=shape) + (1j * rng.normal(size=shape) if cplx_x else 0)
+    dt = np.complex128 if (cplx_A or cplx_x) else np.float64
+    a = 0.7 - 0.2j if dt == np.complex128 else 0.7
+    ref = a * (A @ x)
+    xd = D.to_device(x, dt)
+    y0 = D.to_device(rng.normal(size=shape), dt)
+    for prec in ("double", "ieee"):
+        y = torch.empty_like(xd)
+        M.matvec_into(xd, y, a=a, overwrite=True, precision=prec)
+        assert _rel(D.to_host(y), ref) <= 1e-13, prec
+        yacc = y0.clone()
+        M.matvec_into(xd, yacc, a=a, overwrite=False, precision=prec)
+        assert _rel(D.to_host(yacc), D.to_host(y0) + ref) <= 1e-13, prec
+
+
+@pytest.mark.parametrize("scale", [1e-300, 1e-45, 1e45, 1e300])
+def test_pair_form_scaled_inputs(cuda, scale):
+    import torch
+    from quspin_gb300 import _device as D
+    from quspin_gb300.sparse import DeviceCSR
+    n = 20000
+    A = _mat(n, True, 3) * 0.5
+    M = DeviceCSR.from_scipy(A)
+    rng = np.random.default_rng(4)
+    x = (rng.normal(size=n) + 1j * rng.normal(size=n)) * scale
+    xd = D.to_device(x, np.complex128)
+    y = torch.empty_like(xd)
+    M.matvec_into(xd, y, precision="double")
+    yh = D.to_host(y)
+    assert np.all(np.isfinite(yh))
+    assert _rel(yh, A @ x) <= 1e-13
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_single_precision_form(cuda, cplx):
+    import torch
+    from quspin_gb300 import _device as D
+    from quspin_gb300.sparse import DeviceCSR
+    n = 50000
+    A = _mat(n, cplx, 5)
+    M = DeviceCSR.from_scipy(A).astype(np.complex64 if cplx else np.float32)
+    rng = np.random.default_rng(6)
+    x = rng.normal(size=(n, 4)) + 1j * rng.normal(size=(n, 4))
+    xd = D.to_device(x, np.complex64)
+    y = torch.empty_like(xd)
+    M.matvec_into(xd, y, a=1.5)
+    assert y.dtype == torch.complex64
+    assert _rel(D.to_host(y), 1.5 * (A @ x)) <= 2e-6
+
+
+def test_hamiltonian_dot_default_form(cuda):
+    """hamiltonian.dot through the default (float-pair) product agrees with
+    the IEEE product to 1e-13."""
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    from quspin_gb300.sparse import set_spmv_precision
+    from tests.models import chain_maps, j1j2_static
+    L = 20
+    m = chain_maps(L)
+    b = spin_basis_general(L, Nup=L // 2, kblock=(m["t"], 0), pblock=(m["p"], 0), zblock=(m["z"], 0), pauli=0)
+    H = hamiltonian(j1j2_static(L), [], basis=b, dtype=np.float64)
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=H.Ns) + 1j * rng.normal(size=H.Ns)
+    w = H.dot(v)
+    old = set_spmv_precision("ieee")
+    try:
+        wi = H.dot(v)
+    finally:
+        set_spmv_precision(old)
+    assert _rel(w, wi) <= 1e-13
+    assert _rel(w, H.tocsr() @ v) <= 1e-13
