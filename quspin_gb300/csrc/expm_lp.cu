@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
     using S = typename M::S;
     using BE = typename M::BE;
     constexpr int NS = MULTI ? QS_MAX_SECTORS : 1;
-    __shared__ S s_mu[2 * NS];
+    __shared__ S s_cm[2 * NS];       // cf * mu per sector (the shift folded into the coefficient)
     __shared__ S s_cf[2];
     __shared__ int s_bexp[NS];
     __shared__ int s_done[NS];
@@ -60,8 +60,12 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
             s_bexp[0] = *((volatile int *)&ctl->bexp);
             s_done[0] = 0;
         }
-        if (threadIdx.x == 1) s_mu[0] = M::from_d(mu0.x);
-        if (threadIdx.x == 2) s_mu[1] = M::from_d(mu0.y);
+        if (threadIdx.x == 1) {
+            const cx<S> c{M::from_d(coeff[j].x), M::from_d(coeff[j].y)};
+            const cx<S> m{M::from_d(mu0.x), M::from_d(mu0.y)};
+            s_cm[0] = M::sub(M::mul(c.re, m.re), M::mul(c.im, m.im));
+            s_cm[1] = M::add(M::mul(c.re, m.im), M::mul(c.im, m.re));
+        }
     } else {
         MultiCtl *ctl = reinterpret_cast<MultiCtl *>(ctlp);
         nsec = ctl->nsec;
@@ -69,9 +73,11 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
         for (int b = threadIdx.x; b < nsec; b += blockDim.x) {
             s_done[b] = *((volatile int *)&ctl->done[b]);
             s_bexp[b] = ctl->bexp[b];
-            const cdbl m = mus[b];
-            s_mu[2 * b] = M::from_d(m.x);
-            s_mu[2 * b + 1] = M::from_d(m.y);
+            const cdbl md = mus[b];
+            const cx<S> c{M::from_d(coeff[j].x), M::from_d(coeff[j].y)};
+            const cx<S> m{M::from_d(md.x), M::from_d(md.y)};
+            s_cm[2 * b] = M::sub(M::mul(c.re, m.re), M::mul(c.im, m.im));
+            s_cm[2 * b + 1] = M::add(M::mul(c.re, m.im), M::mul(c.im, m.re));
             s_mb[b] = 0u;
             s_mf[b] = 0u;
         }
@@ -87,7 +93,11 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
     const int gsub = (threadIdx.x & 31) >> lgG;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const cx<S> cf{s_cf[0], s_cf[1]};
+    // lane comp computes component comp of the new term:
+    //   re: cf.re acc.re - cf.im acc.im - (cm.re bo.re - cm.im bo.im)
+    //   im: cf.re acc.im + cf.im acc.re - (cm.re bo.im + cm.im bo.re)
+    const S cf_re = s_cf[0];
+    const S cf_x = comp ? s_cf[1] : M::neg(s_cf[1]);
     float mb = 0.f, mf = 0.f;
     // Rows are handed out per warp (GPW consecutive rows per warp and
     // iteration), so every lane reaches the full-mask shuffles.
@@ -99,7 +109,8 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
         const bool writer = valid && lane < 2;
         const IT k0 = valid ? indptr[r] : (IT)0, k1 = valid ? indptr[r + 1] : (IT)0;
         const int bexp = s_bexp[sec];
-        const cx<S> mu{s_mu[2 * sec], s_mu[2 * sec + 1]};
+        const S cm_re = s_cm[2 * sec];
+        const S cm_x = comp ? s_cm[2 * sec + 1] : M::neg(s_cm[2 * sec + 1]);
         float rbn = 0.f, rfn = 0.f;
         BE bo_pre{M::zero(), M::zero()};
         double f_pre = 0.0;
@@ -143,16 +154,15 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
                 if (c0 + b >= nvec) break;
                 const int64_t e = r * nvec + c0 + b;
                 const BE bo = NB == 1 ? bo_pre : (writer ? M::ldB(Bin + e) : BE{M::zero(), M::zero()});
-                const S accr = M::fin(ar[b]), acci = M::fin(ai[b]);
-                // w = A B - mu B;  new term = cf w
-                const S wr = M::sub(accr, M::sub(M::mul(mu.re, bo.re), M::mul(mu.im, bo.im)));
-                const S wi = M::sub(acci, M::add(M::mul(mu.re, bo.im), M::mul(mu.im, bo.re)));
-                const S bnr = M::sub(M::mul(cf.re, wr), M::mul(cf.im, wi));
-                const S bni = M::add(M::mul(cf.re, wi), M::mul(cf.im, wr));
-                const float nb2 = M::hi(bnr) * M::hi(bnr) + M::hi(bni) * M::hi(bni);
+                // new term = cf (A B) - (cf mu) B, this lane's component only
+                const S acc_c = M::fin(comp ? ai[b] : ar[b]), acc_o = M::fin(comp ? ar[b] : ai[b]);
+                const S bo_c = comp ? bo.im : bo.re, bo_o = comp ? bo.re : bo.im;
+                const S mine = M::sub(M::add(M::mul(cf_re, acc_c), M::mul(cf_x, acc_o)),
+                                      M::add(M::mul(cm_re, bo_c), M::mul(cm_x, bo_o)));
+                float nb2 = M::hi(mine) * M::hi(mine);
+                nb2 += __shfl_xor_sync(0xffffffffu, nb2, 1);
                 float fc = 0.f;
                 if (writer) {
-                    const S mine = comp ? bni : bnr;
                     M::st_comp(Bout + e, comp, mine);
                     double *fp = reinterpret_cast<double *>(F + e) + comp;
                     double fv = NB == 1 ? f_pre : __ldcs(fp);
