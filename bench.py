@@ -599,7 +599,9 @@ def run_hubbard(args):
     v0 = torch.tensor(rng.normal(size=b.Ns) + 0j, device="cuda")
     m = 150
     res = {}
-    for prec in ("double", "mixed"):
+    from quspin_gb300.sparse import set_spmv_precision
+    for label, prec, spmv in (("ieee", "double", "ieee"), ("double", "double", "double"), ("mixed", "mixed", "double")):
+        old = set_spmv_precision(spmv)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         E, V, Q = lanczos_full(H4, v0, m, reorth=True, precision=prec)
@@ -607,15 +609,19 @@ def run_hubbard(args):
         el = time.perf_counter() - t0
         g = lin_comb_Q_T(V[:, 0], Q)
         g = g / torch.linalg.vector_norm(g)
-        res[prec] = {"E": E[:4].tolist(), "seconds": el, "ground": g}
-    psi0 = res["double"]["ground"]
-    e_err = [abs(a - b_) for a, b_ in zip(res["mixed"]["E"], res["double"]["E"])]
-    st_err = float(torch.linalg.vector_norm(res["mixed"]["ground"] * torch.vdot(res["mixed"]["ground"], psi0).sgn().conj()
-                                            - psi0))
+        set_spmv_precision(old)
+        res[label] = {"E": E[:4].tolist(), "seconds": el, "ground": g}
+    psi0 = res["ieee"]["ground"]
+    lz = {}
+    for label, r in res.items():
+        gs = r["ground"] * torch.vdot(r["ground"], psi0).sgn().conj()
+        lz[label] = {"E0..3": r["E"], "seconds": r["seconds"],
+                     "abs_energy_error_vs_ieee": [abs(a - b_) for a, b_ in zip(r["E"], res["ieee"]["E"])],
+                     "ground_state_error_vs_ieee": float(torch.linalg.vector_norm(gs - psi0))}
     # quench: 100 steps of dt = 0.1 under U = 8
     q = {}
     A8 = H8.tocsr_gpu()
-    for prec in ("double", "mixed"):
+    for prec in ("ieee", "double", "mixed"):
         op = ExpmMultiplyParallel(A8, a=-0.1j, precision=prec)
         F = psi0.clone()
         torch.cuda.synchronize()
@@ -624,13 +630,46 @@ def run_hubbard(args):
             op.dot(F, overwrite_v=True)
         torch.cuda.synchronize()
         q[prec] = {"seconds": time.perf_counter() - t0, "F": F}
-    q_err = float(torch.linalg.vector_norm(q["mixed"]["F"] - q["double"]["F"]) / torch.linalg.vector_norm(q["double"]["F"]))
+    qo = {p_: {"seconds": v_["seconds"], "rel_state_error_vs_ieee": float(
+        torch.linalg.vector_norm(v_["F"] - q["ieee"]["F"]) / torch.linalg.vector_norm(q["ieee"]["F"]))}
+        for p_, v_ in q.items()}
     out = {"workload": "hubbard_4x4_Nf5_5_k00", "Ns": b.Ns, "nnz": int(H4.tocsr_gpu().nnz), "build_s": t_build,
-           "lanczos_m": m, "lanczos_fp64": {"E0..3": res["double"]["E"], "seconds": res["double"]["seconds"]},
-           "lanczos_mixed": {"E0..3": res["mixed"]["E"], "seconds": res["mixed"]["seconds"],
-                             "abs_energy_error_vs_fp64": e_err, "ground_state_error_vs_fp64": st_err},
-           "quench_fp64_seconds": q["double"]["seconds"], "quench_mixed_seconds": q["mixed"]["seconds"],
-           "quench_mixed_rel_state_error_vs_fp64": q_err}
+           "lanczos_m": m, "lanczos": lz, "quench_100_steps_dt0.1": qo}
+    print(json.dumps(out))
+
+
+def run_lanczos(args):
+    """Lanczos at GPU scale: the J1-J2 chain L=32 (Sz=0, k=0, p=+1, z=+1,
+    4,707,969 states), 200 iterations with full reorthogonalisation from a
+    seeded real Gaussian start vector; IEEE-double SpMV vs the float-pair
+    SpMV, the recurrence and reorthogonalisation in FP64 for both."""
+    import torch
+    from quspin_gb300.sparse import set_spmv_precision
+    from quspin_gb300.tools import lanczos_full
+    L = args.L
+    t0 = time.perf_counter()
+    b, H = build_problem(L, 1.0, 0.5)
+    A = H.tocsr_gpu()
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    v0 = torch.tensor(rng.normal(size=A.shape[0]), dtype=torch.float64, device="cuda")
+    m = 200
+    res = {}
+    for spmv in ("ieee", "double"):
+        old = set_spmv_precision(spmv)
+        lanczos_full(A, v0, 10, reorth=True)          # warm-up (tuning, buffers)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, V, Q = lanczos_full(A, v0, m, reorth=True)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        set_spmv_precision(old)
+        res[spmv] = {"E0": float(E[0]), "E1": float(E[1]), "seconds": el, "iterations_per_s": m / el}
+        del Q
+    res["double"]["abs_E0_error_vs_ieee"] = abs(res["double"]["E0"] - res["ieee"]["E0"])
+    out = {"workload": "j1j2_chain_L{}_lanczos_200_reorth".format(L), "Ns": A.shape[0], "nnz": A.nnz,
+           "build_s": t_build, "m": m, "spmv_ieee": res["ieee"], "spmv_float_pairs": res["double"]}
     print(json.dumps(out))
 
 
@@ -694,7 +733,7 @@ def main():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
     p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
-    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard"],
+    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard", "lanczos"],
                    help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
     if args.L != 32 and args.workload == "j1j2":
@@ -710,6 +749,9 @@ def main():
         return
     if args.workload == "hubbard":
         run_hubbard(args)
+        return
+    if args.workload == "lanczos":
+        run_lanczos(args)
         return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")
