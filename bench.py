@@ -182,49 +182,62 @@ def spmv_bytes(n, nnz, nvec=1):
     return nnz * (8 + 4) + 4 * (n + 1) + n * nvec * (16 + 16)
 
 
-def time_kernels(op, F, reps=20):
-    """Average device time of the Taylor-term kernel launched alone (stopping
-    test disabled) in the operator's precision and in IEEE double, and of the
-    plain SpMV; CUDA events on the launching stream."""
+def evolution_term_times(op, F):
+    """Per-launch device times of the fused Taylor-term kernel inside one real
+    evolution of F (the launch sequence of qs_expm_multiply replayed with a
+    CUDA event pair around every launch, in the operator's current precision).
+    Returns (mean ms of the launches that executed a term, executed terms,
+    launch shape).  Launches after a substep's stopping test fired return at
+    once and are counted apart."""
     import torch
     from quspin_gb300 import _device as D
     from quspin_gb300 import _lib
     from quspin_gb300.tune import tune_taylor
-    A = op.A_device
-    n = A.shape[0]
-    st = torch.cuda.current_stream()
-    mu = complex(op._mu)
-    one = torch.ones(1, dtype=torch.complex128, device=F.device)
-
-    def term_time(M, btype):
-        work = torch.empty(2 * n, dtype=torch.complex64 if btype == _lib.C64 else torch.complex128, device=F.device)
-        b0, b1 = work[:n], work[n:]
-        Fw = F.clone()
-        ctl = torch.zeros(6, dtype=torch.int64, device=F.device)
-        _lib.call("qs_taylor_rescale", n, 1, D.ptr(Fw), D.ptr(b0), btype, D.ptr(one), D.ptr(ctl), 0, D.stream())
-        ctl.view(torch.float64)[0] = float("inf")          # c1 = inf and tol = 0: the stopping test never fires
-        coeff = torch.tensor([complex(op.a) / 1000.0], dtype=torch.complex128, device=F.device)
-        group = tune_taylor(M, 1, btype)
-
-        def launch(j):
-            bi, bo = (b0, b1) if j % 2 == 0 else (b1, b0)
-            _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
-                      M.vcode, D.ptr(bi), D.ptr(bo), btype, D.ptr(Fw), 1, mu.real, mu.imag, D.ptr(coeff),
-                      0, 0.0, D.ptr(ctl), group, D.stream())
-        for j in range(3):
-            launch(j)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        for j in range(reps):
-            launch(j)
-        e1.record(st)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1e3 / reps, group
-
+    n = op.A_device.shape[0]
     M, bt = op._operand()
-    t_term, group = term_time(M, bt)
-    t_ieee, group_ieee = term_time(A, _lib.C128)
+    group = tune_taylor(M, 1, bt)
+    wbuf, ctl = op._buffers(n, 1, bt)
+    a, mu, s, m = complex(op.a), complex(op._mu), op.s, op.m_star
+    coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], np.complex128)
+    consts = D.to_device(np.concatenate([coeff, [np.exp(a * mu / s), 1.0]]).astype(np.complex128))
+    k = max(m, 1)
+    b0, b1 = wbuf[:n], wbuf[n:2 * n]
+    Fw = F.clone()
+    ctl.zero_()
+    _lib.call("qs_taylor_rescale", n, 1, D.ptr(Fw), D.ptr(b0), bt, D.ptr(consts[k + 1:]), D.ptr(ctl), 0, D.stream())
+    evs = []
+    for _ in range(s):
+        for j in range(m):
+            bi, bo = (b0, b1) if j % 2 == 0 else (b1, b0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
+                      M.vcode, D.ptr(bi), D.ptr(bo), bt, D.ptr(Fw), 1, mu.real, mu.imag, D.ptr(consts[:k]), j,
+                      float(op._tol), D.ptr(ctl), group, D.stream())
+            e1.record()
+            evs.append((e0, e1))
+        _lib.call("qs_taylor_rescale", n, 1, D.ptr(Fw), D.ptr(b0), bt, D.ptr(consts[k:k + 1]), D.ptr(ctl), 1,
+                  D.stream())
+    torch.cuda.synchronize()
+    ts = np.array([e0.elapsed_time(e1) for e0, e1 in evs])
+    executed = int(ctl[4].item())
+    live = np.sort(ts)[::-1][:executed]          # early-exit launches take microseconds
+    return float(live.mean()), executed, group
+
+
+def time_kernels(op, F, reps=20):
+    """Per-launch device time of the Taylor-term kernel inside a real
+    evolution, in the operator's precision and in IEEE double, and of the
+    plain SpMV; CUDA events on the launching stream."""
+    import torch
+    A = op.A_device
+    st = torch.cuda.current_stream()
+    prec = op.precision
+    t_term, _, group = evolution_term_times(op, F)
+    op.precision = "ieee"
+    t_ieee, _, group_ieee = evolution_term_times(op, F)
+    op.precision = prec
+    t_term, t_ieee = t_term / 1e3, t_ieee / 1e3
     y = torch.empty_like(F)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for _ in range(3):
@@ -366,7 +379,8 @@ def run_ours(args, rank, ws):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_lp_kernel",
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
-                     "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff},
+                     "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff,
+                                      "six_blocks_per_sm": (group >> 16) & 1},
                      "spmv_gbs": spmv_bytes(n, nnz) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv},
         "gpu_launches": int(args.steps * launches_per_evolution),
         "clocks": clk.summary(),

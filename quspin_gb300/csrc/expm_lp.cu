@@ -34,7 +34,7 @@ namespace {
 // One Taylor term; MULTI: block-diagonal stack of sectors (MultiCtl), else one
 // matrix (ExpmCtl).  lgG: log2 of the lanes per row.
 template <class M, class DV, class IT, int NB, int U, bool MULTI>
-__global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, const IT *__restrict__ indptr,
+__device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__restrict__ indptr,
                                                         const int32_t *__restrict__ indices,
                                                         const DV *__restrict__ data,
                                                         const typename M::BE *__restrict__ Bin,
@@ -244,6 +244,28 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(int64_t n, int lgG, cons
     }
 }
 
+#define TAYLOR_LP_PARAMS                                                                                      \
+    int64_t n, int lgG, const IT *__restrict__ indptr, const int32_t *__restrict__ indices,                   \
+        const DV *__restrict__ data, const typename M::BE *__restrict__ Bin, typename M::BE *__restrict__ Bout, \
+        cdbl *__restrict__ F, int64_t nvec, cdbl mu0, const cdbl *__restrict__ mus,                           \
+        const int64_t *__restrict__ sec_off, const cdbl *__restrict__ coeff, int j, double tol, void *ctlp
+#define TAYLOR_LP_ARGS n, lgG, indptr, indices, data, Bin, Bout, F, nvec, mu0, mus, sec_off, coeff, j, tol, ctlp
+
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
+__global__ void __launch_bounds__(256) taylor_lp_kernel(TAYLOR_LP_PARAMS)
+{
+    taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
+}
+
+// The same term with registers capped for six resident blocks per SM (48
+// warps instead of 40 for the one-column shapes): more gathers in flight per
+// SM for the latency-bound single-vector case; the tuner decides per matrix.
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
+__global__ void __launch_bounds__(256, 6) taylor_lp_kernel_occ(TAYLOR_LP_PARAMS)
+{
+    taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
+}
+
 // F = eta F (per sector for MULTI) and the row-norm maximum; the last block
 // sets c1 = ||F||_inf, the storage exponent bexp and clears the per-substep
 // state (counting, at a substep end, a stopping test that never fired).
@@ -357,15 +379,20 @@ __global__ void split_pairs_kernel(int64_t count, const double *__restrict__ src
     }
 }
 
-template <class M, class DV, class IT, int NB, int U, bool MULTI>
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool OCC = false>
 int lp_go(const LpTerm &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
     const int blocks = taylor_grid(a.n, a.G);
-    taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
-        a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-        (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
+    if constexpr (OCC)
+        taylor_lp_kernel_occ<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
+            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
+    else
+        taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
+            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
@@ -375,6 +402,12 @@ int lp_nb(const LpTerm &a)
 {
     if (a.nvec == 1) {
         if constexpr (sizeof(IT) == 4) {
+            if constexpr (!MULTI) {
+                if (a.occ) {
+                    if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, false, true>(a);
+                    return lp_go<M, DV, IT, 1, 1, false, true>(a);
+                }
+            }
             if (a.U >= 4 && !MULTI) return lp_go<M, DV, IT, 1, 4, MULTI>(a);
             if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, MULTI>(a);
         }

@@ -18,8 +18,8 @@ from . import _lib
 MIN_ROWS = 65536
 
 
-def encode(G, U):
-    return int(G) | (int(U) << 8)
+def encode(G, U, occ=0):
+    return int(G) | (int(U) << 8) | (int(occ) << 16)
 
 
 def _candidates(n, nnz, nvec):
@@ -85,8 +85,12 @@ def tune_taylor(M, nvec, btype):
     ctl = torch.zeros(6, dtype=torch.int64, device=D.device())
     coeff = torch.tensor([1e-3 + 0j], dtype=torch.complex128, device=D.device())
     best, best_t = 0, None
-    for G, U in _candidates(n, M.nnz, nvec):
-        code = encode(G, U)
+    cands = [(G, U, 0) for G, U in _candidates(n, M.nnz, nvec)]
+    if btype != _lib.C128 and nvec == 1:
+        # register-capped variant (more resident warps) of the float forms
+        cands += [(G, U, 1) for G, U, _ in cands if U <= 2]
+    for G, U, occ in cands:
+        code = encode(G, U, occ)
 
         def run():
             _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
