@@ -154,6 +154,18 @@ int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, co
                      double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
                      void *d_work, int btype, void *d_ctl, int group, void *stream);
 
+/* ---- Runge-Kutta stage arithmetic of hamiltonian.evolve: replaces the
+ * state updates of scipy's DOP853 that the reference drives through
+ * src/quspin/tools/evolution.py:300-345 (hamiltonian_core.py:1489-1630 builds
+ * the right-hand side).  The state is viewed as n2 real components; K holds
+ * nk stage derivatives of n2 doubles; coefficient arrays are host memory. --- */
+int qs_rk_error_scratch_doubles(int64_t n2);
+int qs_rk_combine(int64_t n2, const double *d_y, const double *d_K, int nk, const double *c_host, double h,
+                  double *d_out, void *stream);
+int qs_rk_error(int64_t n2, const double *d_y0, const double *d_y1, const double *d_K, int nk,
+                const double *e5_host, const double *e3_host, double atol, double rtol, double *d_scratch,
+                double *d_out, void *stream);
+
 /* ---- many sectors in one launch: block-diagonal stack of sector matrices,
  * per-sector shift / factor / stopping test, common (s, m*) schedule.  The
  * reference fans sectors out to processes (src/quspin/tools/block_tools.py:

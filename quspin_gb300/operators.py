@@ -283,6 +283,14 @@ class hamiltonian:
     def todense(self, time=0):
         return self.tocsr(time).todense()
 
+    def evolve(self, v0, t0, times, eom="SE", solver_name="dop853", stack_state=False, verbose=False,
+               iterate=False, imag_time=False, **solver_args):
+        """(Imaginary-)time Schroedinger evolution (hamiltonian_core.py:1489-1630),
+        integrated by DOP853 on the device (tools/evolution.py)."""
+        from .tools.evolution import evolve_hamiltonian
+        return evolve_hamiltonian(self, v0, t0, times, eom=eom, solver_name=solver_name, stack_state=stack_state,
+                                  verbose=verbose, iterate=iterate, imag_time=imag_time, **solver_args)
+
     def tocsr_gpu(self, time=0):
         """Device CSR of H(time).  The union sparsity pattern of the static and
         dynamic parts is built once; each call forms the values on the device."""
