@@ -290,9 +290,9 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // QS_CPF, values split by qs_split_pairs) or QS_C64 (dtype QS_F32 / QS_C64);
 // F is complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
 // ctl: device control block (qs_expm_ctl_bytes()).  group: launch shape,
-// G | (U << 8) | (O << 16) (G lanes per row 2..32, U = 1, 2, 4 entries in flight
-// per lane, O = 1 for the register-capped variant of the float forms with one
-// column and int32 indptr; ignored elsewhere);
+// G | (U << 8) | (C << 16) (G lanes per row 2..32, U = 1, 2, 4 entries in flight
+// per lane, C = 1 for contiguous row runs per warp with bulk L2 prefetch in the
+// float forms with one column and int32 indptr; ignored elsewhere);
 // 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                               const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,

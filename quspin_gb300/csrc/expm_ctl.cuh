@@ -117,7 +117,7 @@ struct LpTerm {
     double tol;
     void *ctl;
     int G, U;
-    int occ;                  // 1: the register-capped six-blocks-per-SM variant (one column, int32 indptr)
+    int chunk;                // 1: contiguous row runs per warp with bulk L2 prefetch (one column, int32 indptr)
     cudaStream_t st;
 };
 

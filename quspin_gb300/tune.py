@@ -18,8 +18,8 @@ from . import _lib
 MIN_ROWS = 65536
 
 
-def encode(G, U, occ=0):
-    return int(G) | (int(U) << 8) | (int(occ) << 16)
+def encode(G, U, chunk=0):
+    return int(G) | (int(U) << 8) | (int(chunk) << 16)
 
 
 def _candidates(n, nnz, nvec):
@@ -87,8 +87,8 @@ def tune_taylor(M, nvec, btype):
     best, best_t = 0, None
     cands = [(G, U, 0) for G, U in _candidates(n, M.nnz, nvec)]
     if btype != _lib.C128 and nvec == 1:
-        # register-capped variant (more resident warps) of the float forms
-        cands += [(G, U, 1) for G, U, _ in cands if U <= 2]
+        # contiguous row runs with bulk L2 prefetch (float forms)
+        cands += [(G, U, 1) for G, U, _ in cands]
     for G, U, occ in cands:
         code = encode(G, U, occ)
 
