@@ -687,6 +687,73 @@ def run_lanczos(args):
     print(json.dumps(out))
 
 
+def run_evolve(args):
+    """hamiltonian.evolve on the device: the driven Ising chain of the learned
+    workload (L=26, k=0, p=+1), one state over one drive period with the
+    reference's default tolerances (rtol = atol = 1e-9), against the same
+    integration at rtol = atol = 1e-12 (error) and the reference's integrator
+    (scipy ode DOP853 over a scipy CSR right-hand side) on the host for a
+    bounded sample, scaled per right-hand-side evaluation."""
+    import torch
+    from scipy.integrate import ode
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    from quspin_gb300.tools.evolution import DeviceDOP853
+    L = args.L if args.L != 32 else 26
+    s_ = np.arange(L)
+    b = spin_basis_general(L, kblock=((s_ + 1) % L, 0), pblock=(s_[::-1].copy(), 0))
+    static = [["zz", [[-1.0, i, (i + 1) % L] for i in range(L)]], ["z", [[-0.2, i] for i in range(L)]]]
+    drive = lambda t, h0, A, w: h0 + A * np.cos(w * t)
+    dyn = [["x", [[-1.0, i] for i in range(L)], drive, (0.8, 0.5, 2 * np.pi)]]
+    H = hamiltonian(static, dyn, basis=b, dtype=np.float64)
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=H.Ns) + 1j * rng.normal(size=H.Ns)
+    v /= np.linalg.norm(v)
+    vd = torch.tensor(v, device="cuda")
+    T = 1.0
+    res = {}
+    for tol in (1e-9, 1e-12):
+        sol = DeviceDOP853(lambda t, y, out: H.dot(y, time=t, out=out, a=-1j), vd, 0.0, rtol=tol, atol=tol)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        y = sol.integrate(T).clone()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        res[tol] = {"seconds": el, "rhs_evaluations": sol.nfev, "accepted_steps": sol.naccept,
+                    "rejected_steps": sol.nreject, "y": y}
+    err = float(torch.linalg.vector_norm(res[1e-9]["y"] - res[1e-12]["y"]))
+    # the reference's integrator on the host: scipy ode DOP853 over scipy CSR products, bounded sample
+    A0 = H.static.tocsr()
+    A1 = list(H.dynamic.values())[0].tocsr()
+    f = list(H.dynamic.keys())[0]
+
+    calls = [0]
+
+    def rhs(t, yr):
+        calls[0] += 1
+        yc = yr.view(np.complex128)
+        return (-1j * (A0 @ yc + f(t) * (A1 @ yc))).view(np.float64)
+    solver = ode(rhs)
+    solver.set_integrator("dop853", rtol=1e-9, atol=1e-9, nsteps=np.iinfo(np.int32).max)
+    solver.set_initial_value(np.ascontiguousarray(v).view(np.float64), 0.0)
+    t0 = time.perf_counter()
+    t_s = 0.0
+    while time.perf_counter() - t0 < 15.0 and t_s < T:
+        t_s = min(T, t_s + 0.002)
+        solver.integrate(t_s)
+    el_cpu = time.perf_counter() - t0
+    per_eval_cpu = el_cpu / max(calls[0], 1)
+    r9 = res[1e-9]
+    out = {"workload": "evolve_driven_ising_L{}_one_period".format(L), "Ns": H.Ns, "t": T,
+           "gpu": {"seconds": r9["seconds"], "rhs_evaluations": r9["rhs_evaluations"],
+                   "accepted_steps": r9["accepted_steps"], "rejected_steps": r9["rejected_steps"],
+                   "ms_per_rhs": 1e3 * r9["seconds"] / r9["rhs_evaluations"]},
+           "state_error_vs_tol_1e-12": err,
+           "cpu_reference_integrator": {"ms_per_rhs": 1e3 * per_eval_cpu, "sample_rhs": calls[0],
+                                        "sample_t": t_s, "estimated_seconds": per_eval_cpu * r9["rhs_evaluations"],
+                                        "note": "scipy ode DOP853, scipy CSR products, one host thread"}}
+    print(json.dumps(out))
+
+
 def run_reference(args, rank, ws):
     """The reference's CPU path (the oracle port of QuSpin's OpenMP basis,
     CSR assembly and Taylor loop) on the host cores; each step a bounded
@@ -747,7 +814,8 @@ def main():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
     p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
-    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard", "lanczos"],
+    p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard", "lanczos",
+                                                           "evolve"],
                    help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
     if args.L != 32 and args.workload == "j1j2":
@@ -766,6 +834,9 @@ def main():
         return
     if args.workload == "lanczos":
         run_lanczos(args)
+        return
+    if args.workload == "evolve":
+        run_evolve(args)
         return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")
