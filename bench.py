@@ -379,8 +379,7 @@ def run_ours(args, rank, ws):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_lp_kernel",
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
-                     "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff,
-                                      "row_runs_l2_prefetch": (group >> 16) & 1},
+                     "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff},
                      "spmv_gbs": spmv_bytes(n, nnz) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv},
         "gpu_launches": int(args.steps * launches_per_evolution),
         "clocks": clk.summary(),

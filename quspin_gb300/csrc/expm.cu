@@ -290,9 +290,7 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // QS_CPF, values split by qs_split_pairs) or QS_C64 (dtype QS_F32 / QS_C64);
 // F is complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
 // ctl: device control block (qs_expm_ctl_bytes()).  group: launch shape,
-// G | (U << 8) | (C << 16) (G lanes per row 2..32, U = 1, 2, 4 entries in flight
-// per lane, C = 1 for contiguous row runs per warp with bulk L2 prefetch in the
-// float forms with one column and int32 indptr; ignored elsewhere);
+// G | (U << 8) (G lanes per row 2..32, U = 1, 2, 4 entries in flight per lane);
 // 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                               const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
@@ -305,7 +303,6 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
     if (U < 1) U = 1;
     if (G != 2 && G != 4 && G != 8 && G != 16 && G != 32) return QS_ERR_ARG;
     if (U != 1 && U != 2 && U != 4) return QS_ERR_ARG;
-    if (group > 0 && (group >> 17) != 0) return QS_ERR_ARG;
     cdbl mu{mu_re, mu_im};
     cudaStream_t st = qs_stream(stream);
     ExpmCtl *c = reinterpret_cast<ExpmCtl *>(ctl);
@@ -313,7 +310,7 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
     if (lp_btype(btype)) {
         LpTerm a{n, indptr, idx64, indices, data, dtype, Bin, Bout, btype, Fp, nvec, mu, nullptr, nullptr, cf, j, tol,
-                 ctl, G, U, group > 0 ? (group >> 16) & 1 : 0, st};
+                 ctl, G, U, st};
         return lp_taylor_term(a, false);
     }
     if (btype == QS_C128) {
@@ -604,7 +601,7 @@ extern "C" int qs_taylor_multi_term(int64_t n, const void *indptr, const int32_t
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
     if (lp_btype(btype)) {
         LpTerm a{n, indptr, 0, indices, data, dtype, Bin, Bout, btype, Fp, nvec, cdbl{0.0, 0.0}, m, sec_off, cf, j, tol,
-                 ctl, G, U, 0, st};
+                 ctl, G, U, st};
         return lp_taylor_term(a, true);
     }
     if (btype == QS_C128) {

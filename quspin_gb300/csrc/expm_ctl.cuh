@@ -117,7 +117,6 @@ struct LpTerm {
     double tol;
     void *ctl;
     int G, U;
-    int chunk;                // 1: contiguous row runs per warp with bulk L2 prefetch (one column, int32 indptr)
     cudaStream_t st;
 };
 

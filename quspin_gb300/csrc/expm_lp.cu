@@ -33,17 +33,7 @@ namespace {
 
 // One Taylor term; MULTI: block-diagonal stack of sectors (MultiCtl), else one
 // matrix (ExpmCtl).  lgG: log2 of the lanes per row.
-// L2 prefetch of the 16-byte-aligned interior of [a, b) (a bulk copy engine
-// request; nothing outside the range is touched)
-__device__ __forceinline__ void l2_prefetch(const void *a, const void *b)
-{
-    const size_t ga = __cvta_generic_to_global(a), gb = __cvta_generic_to_global(b);
-    const size_t lo = (ga + 15) & ~(size_t)15, hi = gb & ~(size_t)15;
-    if (hi > lo)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
-}
-
-template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CHUNK = false>
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
 __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__restrict__ indptr,
                                                         const int32_t *__restrict__ indices,
                                                         const DV *__restrict__ data,
@@ -110,30 +100,10 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
     const S cf_x = comp ? s_cf[1] : M::neg(s_cf[1]);
     float mb = 0.f, mf = 0.f;
     // Rows are handed out per warp (GPW consecutive rows per warp and
-    // iteration), so every lane reaches the full-mask shuffles.  CHUNK: each
-    // warp owns one contiguous run of rows and, while it works on one group,
-    // asks the bulk copy engine to bring the next group's indices, values and
-    // own B / F entries into L2, so the dependent gathers no longer wait
-    // behind an HBM round trip for the column indices.
-    int64_t r_lo = warp * GPW, r_hi = n, r_step = nwarps * GPW;
-    if constexpr (CHUNK) {
-        const int64_t per = ((n + nwarps - 1) / nwarps + GPW - 1) / GPW * GPW;
-        r_lo = warp * per;
-        r_hi = r_lo + per < n ? r_lo + per : n;
-        r_step = GPW;
-    }
-    for (int64_t rb = r_lo; rb < r_hi; rb += r_step) {
+    // iteration), so every lane reaches the full-mask shuffles.
+    const int64_t r_hi = n;
+    for (int64_t rb = warp * GPW; rb < r_hi; rb += nwarps * GPW) {
         const int64_t r = rb + gsub;
-        if constexpr (CHUNK) {
-            if ((threadIdx.x & 31) == 0 && rb + GPW < r_hi) {
-                const int64_t nb = rb + GPW, ne = nb + GPW < r_hi ? nb + GPW : r_hi;
-                const IT ks = indptr[nb], ke = indptr[ne];
-                l2_prefetch(indices + ks, indices + ke);
-                l2_prefetch(data + ks, data + ke);
-                l2_prefetch(Bin + nb * nvec, Bin + ne * nvec);
-                l2_prefetch(F + nb * nvec, F + ne * nvec);
-            }
-        }
         int sec = 0;
         if constexpr (MULTI) sec = r < r_hi ? sector_of(s_off, nsec, r) : 0;
         const bool valid = r < r_hi && !s_done[sec];
@@ -288,14 +258,6 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(TAYLOR_LP_PARAMS)
     taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
 }
 
-// The same term with contiguous row runs per warp and bulk L2 prefetch of
-// the next group (see taylor_lp_body); the tuner decides per matrix.
-template <class M, class DV, class IT, int NB, int U, bool MULTI>
-__global__ void __launch_bounds__(256) taylor_lp_kernel_chunk(TAYLOR_LP_PARAMS)
-{
-    taylor_lp_body<M, DV, IT, NB, U, MULTI, true>(TAYLOR_LP_ARGS);
-}
-
 // F = eta F (per sector for MULTI) and the row-norm maximum; the last block
 // sets c1 = ||F||_inf, the storage exponent bexp and clears the per-substep
 // state (counting, at a substep end, a stopping test that never fired).
@@ -409,20 +371,15 @@ __global__ void split_pairs_kernel(int64_t count, const double *__restrict__ src
     }
 }
 
-template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CHUNK = false>
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
 int lp_go(const LpTerm &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
     const int blocks = taylor_grid(a.n, a.G);
-    if constexpr (CHUNK)
-        taylor_lp_kernel_chunk<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
-            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
-    else
-        taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
-            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
+    taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+        a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
+        (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
@@ -432,13 +389,6 @@ int lp_nb(const LpTerm &a)
 {
     if (a.nvec == 1) {
         if constexpr (sizeof(IT) == 4) {
-            if constexpr (!MULTI) {
-                if (a.chunk) {
-                    if (a.U >= 4) return lp_go<M, DV, IT, 1, 4, false, true>(a);
-                    if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, false, true>(a);
-                    return lp_go<M, DV, IT, 1, 1, false, true>(a);
-                }
-            }
             if (a.U >= 4 && !MULTI) return lp_go<M, DV, IT, 1, 4, MULTI>(a);
             if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, MULTI>(a);
         }

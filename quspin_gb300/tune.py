@@ -18,8 +18,8 @@ from . import _lib
 MIN_ROWS = 65536
 
 
-def encode(G, U, chunk=0):
-    return int(G) | (int(U) << 8) | (int(chunk) << 16)
+def encode(G, U):
+    return int(G) | (int(U) << 8)
 
 
 def _candidates(n, nnz, nvec):
@@ -85,12 +85,8 @@ def tune_taylor(M, nvec, btype):
     ctl = torch.zeros(6, dtype=torch.int64, device=D.device())
     coeff = torch.tensor([1e-3 + 0j], dtype=torch.complex128, device=D.device())
     best, best_t = 0, None
-    cands = [(G, U, 0) for G, U in _candidates(n, M.nnz, nvec)]
-    if btype != _lib.C128 and nvec == 1:
-        # contiguous row runs with bulk L2 prefetch (float forms)
-        cands += [(G, U, 1) for G, U, _ in cands]
-    for G, U, occ in cands:
-        code = encode(G, U, occ)
+    for G, U in _candidates(n, M.nnz, nvec):
+        code = encode(G, U)
 
         def run():
             _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
