@@ -82,19 +82,26 @@ class DeviceDOP853:
         _lib.call("qs_rk_combine", self.n2, D.ptr(self._r(self.y)), D.ptr(self.K), nk,
                   c.ctypes.data, h, D.ptr(self._r(out)), D.stream())
 
+    def _sumsq(self, K, coef, nk):
+        """sum_i ((sum_j coef_j K_j)_i / sk_i)^2 with sk = atol + rtol |y_i|
+        (one pass of the error kernel with y as both end points)."""
+        c = np.zeros(nk, np.float64)
+        c[:] = coef
+        y = D.ptr(self._r(self.y))
+        _lib.call("qs_rk_error", self.n2, y, y, D.ptr(K), nk, c.ctypes.data, c.ctypes.data, self.atol, self.rtol,
+                  D.ptr(self._scr), D.ptr(self._err), D.stream())
+        return float(self._err[0].item())
+
     def _initial_step(self, hmax, direction):
-        y, f0 = self._r(self.y), self._r(self.K[0])
-        sk = self.atol + self.rtol * y.abs()
-        dnf = float(((f0 / sk) ** 2).sum())
-        dny = float(((y / sk) ** 2).sum())
+        """Hairer's starting-step heuristic (HNW I, II.4) on the scaled norms."""
+        dnf = self._sumsq(self.K[0], [1.0], 1)
+        dny = self._sumsq(self.y, [1.0], 1)
         h = 1e-6 if (dnf <= 1e-10 or dny <= 1e-10) else 0.01 * np.sqrt(dny / dnf)
         h = min(h, hmax) * direction
-        y1 = self.ytmp
-        self._r(y1).copy_(y + h * f0)
-        f1 = self.K[1]
-        self.rhs(self.t + h, y1, f1)
+        self._combine(np.array([1.0]), 1, h, self.ytmp)          # y + h f0
+        self.rhs(self.t + h, self.ytmp, self.K[1])
         self.nfev += 1
-        der2 = float(torch.sqrt((((self._r(f1) - f0) / sk) ** 2).sum())) / abs(h)
+        der2 = np.sqrt(self._sumsq(self.K, [-1.0, 1.0], 2)) / abs(h)
         der12 = max(abs(der2), np.sqrt(dnf))
         h1 = max(1e-6, abs(h) * 1e-3) if der12 <= 1e-15 else (0.01 / der12) ** (1.0 / 8.0)
         return min(100 * abs(h), h1, hmax) * direction
