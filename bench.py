@@ -686,6 +686,71 @@ def run_lanczos(args):
     print(json.dumps(out))
 
 
+def run_small(args):
+    """The small plain-method configuration: XXZ chain L=20 (Delta = 0.5,
+    Sz=0, k=0, p=+1: 4,752 states).  (a) e^{-iH} v of a seeded normalised
+    Gaussian state, (b) Lanczos lowest eigenvalue with 60 iterations; GPU
+    (IEEE and float-pair) against the oracle port of the reference's CPU path
+    on the host cores, whole evolutions on both sides."""
+    import torch
+    from oracle import oracle as O
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    from quspin_gb300.tools import ExpmMultiplyParallel, lanczos_full
+    L = 20
+    s_ = np.arange(L)
+    blocks = dict(kblock=((s_ + 1) % L, 0), pblock=(s_[::-1].copy(), 0))
+    stat = [["+-", [[0.5, i, (i + 1) % L] for i in range(L)]], ["-+", [[0.5, i, (i + 1) % L] for i in range(L)]],
+            ["zz", [[0.5, i, (i + 1) % L] for i in range(L)]]]
+    H = hamiltonian(stat, [], basis=spin_basis_general(L, Nup=L // 2, pauli=0, **blocks), dtype=np.float64)
+    A = H.tocsr()
+    n = A.shape[0]
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=n) + 1j * rng.normal(size=n)
+    v /= np.linalg.norm(v)
+    reps = 50
+    out = {"workload": "xxz_chain_L20_Sz0_k0_p+1", "Ns": n, "nnz": int(A.nnz)}
+    np.random.seed(0)
+    op = ExpmMultiplyParallel(H.tocsr_gpu(), a=-1j)
+    vd = torch.tensor(v, device="cuda")
+    for prec in ("ieee", "double"):
+        op.precision = prec
+        F = vd.clone()
+        op.run_device(F)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            F.copy_(vd)
+            op.run_device(F)
+        torch.cuda.synchronize()
+        out["expm_gpu_" + prec] = {"evolutions_per_s": reps / (time.perf_counter() - t0)}
+    np.random.seed(0)
+    oop = O.ExpmMultiplyParallelOracle(A, a=-1j)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        w = oop.dot(v)
+    out["expm_cpu_oracle"] = {"evolutions_per_s": reps / (time.perf_counter() - t0), "cores": O.num_threads()}
+    out["expm_rel_error_gpu_vs_oracle"] = float(np.linalg.norm(D_host(op.dot(v)) - w) / np.linalg.norm(w))
+    v0 = rng.normal(size=n)
+    for prec in ("double",):
+        lanczos_full(H, v0, 60)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            E, _, _ = lanczos_full(H, v0, 60)
+        torch.cuda.synchronize()
+        out["lanczos_gpu"] = {"runs_per_s": 10 / (time.perf_counter() - t0), "E0": float(E[0])}
+    t0 = time.perf_counter()
+    for _ in range(10):
+        Eo, _, _ = O.lanczos_full(lambda x: O.csr_matvec(A, x), np.float64, v0, 60)
+    out["lanczos_cpu_oracle"] = {"runs_per_s": 10 / (time.perf_counter() - t0), "E0": float(Eo[0])}
+    out["lanczos_abs_E0_error"] = abs(out["lanczos_gpu"]["E0"] - out["lanczos_cpu_oracle"]["E0"])
+    print(json.dumps(out))
+
+
+def D_host(x):
+    return x if isinstance(x, np.ndarray) else x.cpu().numpy()
+
+
 def run_evolve(args):
     """hamiltonian.evolve on the device: the driven Ising chain of the learned
     workload (L=26, k=0, p=+1), one state over one drive period with the
@@ -814,7 +879,7 @@ def main():
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
     p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
     p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard", "lanczos",
-                                                           "evolve"],
+                                                           "evolve", "small"],
                    help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
     if args.L != 32 and args.workload == "j1j2":
@@ -836,6 +901,9 @@ def main():
         return
     if args.workload == "evolve":
         run_evolve(args)
+        return
+    if args.workload == "small":
+        run_small(args)
         return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")
