@@ -195,19 +195,35 @@ class ExpmMultiplyParallel:
             self._bufs = {key: b}
         return b
 
+    # below this many states x vectors a dot replays a captured launch
+    # sequence (one graph launch instead of about s (m* + 2) kernel launches)
+    GRAPH_MAX_ELEMS = 1 << 18
+
     def run_device(self, F, tol=None, work=None):
         """In place e^{aA} F for a complex128 device tensor F of shape (n,) or
         (n, k).  Returns F.  No host synchronisation."""
         n = self._Ad.shape[0]
         nvec = 1 if F.dim() == 1 else F.shape[1]
         tol = float(self._tol if tol is None else tol)
-        a = complex(self._a)
-        mu = complex(self._mu)
-        s, m = int(self._s), int(self._m_star)
+        if (work is None and n * nvec <= self.GRAPH_MAX_ELEMS and F.is_contiguous()
+                and not torch.cuda.is_current_stream_capturing()):
+            return self._run_graph(F, tol)
         M, btype = self._operand()
         wbuf, ctl = self._buffers(n, nvec, btype)
         if work is not None and btype != _lib.C64:
             wbuf = work          # 16-byte elements: the caller's complex128 work array holds both B buffers
+        self._consts = self._launch(F, tol, wbuf, ctl)     # kept alive until the stream reaches it
+        self._last_ctl = ctl
+        return F
+
+    def _launch(self, F, tol, wbuf, ctl):
+        """The launch sequence of one evolution of F (no host synchronisation)."""
+        n = self._Ad.shape[0]
+        nvec = 1 if F.dim() == 1 else F.shape[1]
+        a = complex(self._a)
+        mu = complex(self._mu)
+        s, m = int(self._s), int(self._m_star)
+        M, btype = self._operand()
         ctl.zero_()
         coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], dtype=np.complex128)
         eta = np.exp(a * mu / s)
@@ -220,8 +236,36 @@ class ExpmMultiplyParallel:
         _lib.call("qs_expm_multiply", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
                   M.vcode, D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, D.ptr(cf), D.ptr(etap),
                   D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), group, D.stream())
+        return consts
+
+    def _run_graph(self, F, tol):
+        n = self._Ad.shape[0]
+        nvec = 1 if F.dim() == 1 else F.shape[1]
+        key = (tuple(F.shape), self._precision, tol, complex(self._a), int(self._s), int(self._m_star))
+        graphs = self.__dict__.setdefault("_graphs", {})
+        ent = graphs.get(key)
+        if ent is None:
+            _, btype = self._operand()
+            Fg = F.clone()
+            wbuf = torch.empty(2 * n * nvec, dtype=torch.complex64 if btype == _lib.C64 else torch.complex128,
+                               device=F.device)
+            ctl = torch.zeros(max(_lib.load().qs_expm_ctl_bytes() // 8, 1) + 1, dtype=torch.int64,
+                              device=F.device)
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self._launch(Fg, tol, wbuf, ctl)          # tuning and first launches outside the capture
+            torch.cuda.current_stream().wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                consts = self._launch(Fg, tol, wbuf, ctl)
+            ent = (g, Fg, wbuf, ctl, consts)
+            graphs[key] = ent
+        g, Fg, _, ctl, _ = ent
+        Fg.copy_(F)
+        g.replay()
+        F.copy_(Fg)
         self._last_ctl = ctl
-        self._consts = consts     # keep alive until the stream reaches it
         return F
 
     @property

@@ -145,3 +145,31 @@ def test_mixed_precision_error(cuda):
     w64 = ExpmMultiplyParallel(H.tocsr_gpu(), a=-1j).dot(v)
     w32 = ExpmMultiplyParallel(H.tocsr_gpu(), a=-1j, precision="mixed").dot(v)
     assert np.linalg.norm(w32 - w64) / np.linalg.norm(w64) < 1e-6
+
+
+def test_graph_replay_matches_direct_launches(cuda):
+    """Small problems replay a captured launch sequence; the result is the
+    same bit for bit as the direct launches, across repeated calls, new a
+    and several right-hand sides."""
+    import torch
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    H = _c1_like(12)
+    rng = np.random.default_rng(12)
+    V = rng.normal(size=(H.Ns, 3)) + 1j * rng.normal(size=(H.Ns, 3))
+    op = ExpmMultiplyParallel(H.tocsr_gpu(), a=-0.9j)
+    for a in (-0.9j, -2.0j):
+        op.set_a(a)
+        for v in (V[:, 0].copy(), V):
+            F1 = torch.tensor(v, device="cuda")
+            op.run_device(F1)                       # graph path (small n)
+            F2 = torch.tensor(v, device="cuda")
+            op.run_device(F2)                       # replayed again
+            old = ExpmMultiplyParallel.GRAPH_MAX_ELEMS
+            ExpmMultiplyParallel.GRAPH_MAX_ELEMS = 0
+            try:
+                F3 = torch.tensor(v, device="cuda")
+                op.run_device(F3)                   # direct launches
+            finally:
+                ExpmMultiplyParallel.GRAPH_MAX_ELEMS = old
+            assert torch.equal(F1, F2) and torch.equal(F1, F3)
+            assert op.terms_executed > 0
