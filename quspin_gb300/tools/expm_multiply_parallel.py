@@ -216,18 +216,26 @@ class ExpmMultiplyParallel:
         self._last_ctl = ctl
         return F
 
-    def _launch(self, F, tol, wbuf, ctl):
-        """The launch sequence of one evolution of F (no host synchronisation)."""
+    def _consts(self):
+        """Device table: the m* term coefficients a / (s (j+1)), eta, 1."""
+        a = complex(self._a)
+        mu = complex(self._mu)
+        s, m = int(self._s), int(self._m_star)
+        coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], dtype=np.complex128)
+        eta = np.exp(a * mu / s)
+        return D.to_device(np.concatenate([coeff, [eta, 1.0 + 0j]]).astype(np.complex128))
+
+    def _launch(self, F, tol, wbuf, ctl, consts=None):
+        """The launch sequence of one evolution of F (no host synchronisation;
+        with a prepared consts table it issues device work only)."""
         n = self._Ad.shape[0]
         nvec = 1 if F.dim() == 1 else F.shape[1]
-        a = complex(self._a)
         mu = complex(self._mu)
         s, m = int(self._s), int(self._m_star)
         M, btype = self._operand()
         ctl.zero_()
-        coeff = np.array([a / (s * (j + 1)) for j in range(max(m, 1))], dtype=np.complex128)
-        eta = np.exp(a * mu / s)
-        consts = D.to_device(np.concatenate([coeff, [eta, 1.0 + 0j]]).astype(np.complex128))
+        if consts is None:
+            consts = self._consts()
         cf = consts[:max(m, 1)]
         etap = consts[max(m, 1):max(m, 1) + 1]
         onep = consts[max(m, 1) + 1:]
@@ -251,14 +259,15 @@ class ExpmMultiplyParallel:
                                device=F.device)
             ctl = torch.zeros(max(_lib.load().qs_expm_ctl_bytes() // 8, 1) + 1, dtype=torch.int64,
                               device=F.device)
+            consts = self._consts()
             side = torch.cuda.Stream()
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):
-                self._launch(Fg, tol, wbuf, ctl)          # tuning and first launches outside the capture
+                self._launch(Fg, tol, wbuf, ctl, consts)  # tuning and first launches outside the capture
             torch.cuda.current_stream().wait_stream(side)
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
-                consts = self._launch(Fg, tol, wbuf, ctl)
+                self._launch(Fg, tol, wbuf, ctl, consts)
             ent = (g, Fg, wbuf, ctl, consts)
             graphs[key] = ent
         g, Fg, _, ctl, _ = ent
