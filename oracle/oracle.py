@@ -591,3 +591,52 @@ def lin_comb_Q_T(coeff, Q_T):
 def expm_lanczos(E, V, Q_T, a=1.0):
     c = V.dot(np.exp(a * E) * V[0, :])
     return lin_comb_Q_T(c, Q_T)
+
+
+def ftlm_static_iteration(O_dict, E, V, Q_T, beta=0):
+    """Finite-temperature Lanczos, one random start (reference
+    src/quspin/tools/lanczos/_FTLM.py:10-109): with p(beta, j) = exp(-beta E_j)
+    and c[a] = sum_j V[0, j] V[a, j] p(beta, j), the iteration returns
+    sum_a c[a] <q_a | O q_0> for every operator and the identity term c[0]."""
+    E = np.asarray(E)
+    V = np.asarray(V)
+    Q = np.asarray(Q_T)
+    p = np.exp(-np.outer(np.atleast_1d(beta), E))
+    c = np.einsum("j,aj,...j->a...", V[0, :], V, p)
+    r = Q[0]
+    res = {}
+    for key, A in O_dict.items():
+        Ar = A @ r
+        res[key] = np.squeeze(sum(c[i, ...] * np.vdot(Q[i], Ar) for i in range(Q.shape[0])))
+    return res, np.squeeze(c[0, ...])
+
+
+def ltlm_static_iteration(O_dict, E, V, Q_T, beta=0):
+    """Low-temperature Lanczos, one random start (reference
+    src/quspin/tools/lanczos/_LTLM.py:9-139): the Krylov states whose
+    Boltzmann weight at the smallest beta is below machine epsilon are
+    dropped (nv), the operator's matrix in the kept Lanczos basis,
+    Ome[i, j] = <q_j | O q_i>, is rotated to the Ritz basis and weighted by
+    c_j = V[0, j] exp(-beta E_j / 2) on both sides; the identity term is
+    sum_j V[0, j]^2 exp(-beta E_j)."""
+    E = np.asarray(E)
+    V = np.asarray(V)
+    Q = np.asarray(Q_T)
+    nv = E.size
+    beta = np.atleast_1d(beta)
+    p = np.exp(-E * beta.min()) * np.abs(V[0, :]).max()
+    mask = p < np.finfo(p.dtype).eps
+    if np.any(mask):
+        nv = int(np.argmax(mask))
+    res = {}
+    for key, A in O_dict.items():
+        AQ = np.stack([A @ Q[i] for i in range(nv)], axis=0)          # rows: O q_i
+        Ome = (AQ @ Q[:nv].conj().T)                                   # [i, j] = <q_j | O q_i>
+        Vn = V[:nv, :nv]
+        pp = np.exp(-np.outer(E[:nv], beta / 2.0))
+        c = np.einsum("j,j...->j...", Vn[0, :], pp)
+        A_diag = Vn.T.dot(Ome.dot(Vn))
+        res[key] = np.squeeze(np.einsum("j...,l...,jl->...", c, c, A_diag))
+    p = np.exp(-np.outer(E[:nv], beta))
+    Id = np.einsum("j,j...->...", V[:nv, :nv][0, :] ** 2, p)
+    return res, np.squeeze(Id)

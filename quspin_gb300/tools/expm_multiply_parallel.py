@@ -216,7 +216,7 @@ class ExpmMultiplyParallel:
         self._last_ctl = ctl
         return F
 
-    def _consts(self):
+    def _const_table(self):
         """Device table: the m* term coefficients a / (s (j+1)), eta, 1."""
         a = complex(self._a)
         mu = complex(self._mu)
@@ -235,7 +235,7 @@ class ExpmMultiplyParallel:
         M, btype = self._operand()
         ctl.zero_()
         if consts is None:
-            consts = self._consts()
+            consts = self._const_table()
         cf = consts[:max(m, 1)]
         etap = consts[max(m, 1):max(m, 1) + 1]
         onep = consts[max(m, 1) + 1:]
@@ -259,7 +259,7 @@ class ExpmMultiplyParallel:
                                device=F.device)
             ctl = torch.zeros(max(_lib.load().qs_expm_ctl_bytes() // 8, 1) + 1, dtype=torch.int64,
                               device=F.device)
-            consts = self._consts()
+            consts = self._const_table()
             side = torch.cuda.Stream()
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):

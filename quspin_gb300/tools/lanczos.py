@@ -21,7 +21,8 @@ from .. import _device as D
 from .. import _lib
 from ..sparse import DeviceCSR, DeviceDIA, to_device_matrix
 
-__all__ = ["lanczos_full", "lanczos_iter", "lin_comb_Q_T", "expm_lanczos"]
+__all__ = ["lanczos_full", "lanczos_iter", "lin_comb_Q_T", "expm_lanczos", "FTLM_static_iteration",
+           "LTLM_static_iteration"]
 
 
 class _DeviceOp:
@@ -301,3 +302,78 @@ def expm_lanczos(E, V, Q_T, a=1.0, out=None):
     """exp(aA) v0 from a Lanczos decomposition (_expm.py:7-52)."""
     c = V.dot(np.exp(a * E) * V[0, :])
     return lin_comb_Q_T(c, Q_T, out=out)
+
+
+def _q_block(Q_T):
+    """Lanczos rows as one device tensor [m, n] (device tensor, array or an
+    iterator of rows such as lanczos_iter's)."""
+    if D.is_device_array(Q_T):
+        return Q_T
+    if isinstance(Q_T, np.ndarray):
+        return D.to_device(Q_T)
+    rows = [r if D.is_device_array(r) else D.to_device(np.asarray(r)) for r in Q_T]
+    return torch.stack(rows, dim=0)
+
+
+def _apply_block(A, X):
+    """A X for a device block X [n, k] through the operator's own dot."""
+    if hasattr(A, "dot"):
+        return A.dot(X)
+    return D.to_device(A @ D.to_host(X))
+
+
+def FTLM_static_iteration(O_dict, E, V, Q_T, beta=0):
+    """One random start of the finite-temperature Lanczos method
+    (src/quspin/tools/lanczos/_FTLM.py:10-109): with p(beta, j) = exp(-beta E_j)
+    and c[a] = sum_j V[0, j] V[a, j] p(beta, j), returns
+    ({key: sum_a c[a] <q_a | O q_0>}, c[0]) for every operator O of O_dict.
+    The overlaps <q_a | O q_0> are one product and one block inner product
+    per operator on the device."""
+    E = np.asarray(D.to_host(E) if D.is_device_array(E) else E)
+    V = np.asarray(D.to_host(V) if D.is_device_array(V) else V)
+    Q = _q_block(Q_T)
+    p = np.exp(-np.outer(np.atleast_1d(beta), E))
+    c = np.einsum("j,aj,...j->a...", V[0, :], V, p)
+    r = Q[0]
+    res = {}
+    for key, A in O_dict.items():
+        Ar = _apply_block(A, r)
+        Qc = Q.to(torch.promote_types(Q.dtype, Ar.dtype))
+        ov = D.to_host(Qc.conj() @ Ar.to(Qc.dtype))                # <q_a | O q_0>, a = 0..m-1
+        res[key] = np.squeeze(np.tensordot(ov, c[:ov.shape[0]], axes=(0, 0)))
+    return res, np.squeeze(c[0, ...])
+
+
+def LTLM_static_iteration(O_dict, E, V, Q_T, beta=0):
+    """One random start of the low-temperature Lanczos method
+    (src/quspin/tools/lanczos/_LTLM.py:9-139): Krylov states whose Boltzmann
+    weight at the smallest beta is below machine epsilon are dropped (nv);
+    the operator's matrix in the kept Lanczos basis, Ome[i, j] =
+    <q_j | O q_i>, comes from one block product O Q^T (all nv columns in one
+    sparse pass) and one dense [nv, n] x [n, nv] product on the device, is
+    rotated to the Ritz basis and weighted by V[0, j] exp(-beta E_j / 2) on
+    both sides; the identity term is sum_j V[0, j]^2 exp(-beta E_j)."""
+    E = np.asarray(D.to_host(E) if D.is_device_array(E) else E)
+    V = np.asarray(D.to_host(V) if D.is_device_array(V) else V)
+    Q = _q_block(Q_T)
+    nv = E.size
+    beta = np.atleast_1d(beta)
+    p = np.exp(-E * beta.min()) * np.abs(V[0, :]).max()
+    mask = p < np.finfo(p.dtype).eps
+    if np.any(mask):
+        nv = int(np.argmax(mask))
+    Qn = Q[:nv]
+    X = Qn.transpose(0, 1).contiguous()                            # [n, nv]: columns q_i
+    Vn = V[:nv, :nv].copy()
+    pp = np.exp(-np.outer(E[:nv], beta / 2.0))
+    cc = np.einsum("j,j...->j...", Vn[0, :], pp)
+    res = {}
+    for key, A in O_dict.items():
+        AX = _apply_block(A, X)                                    # [n, nv]: columns O q_i
+        dt = torch.promote_types(Qn.dtype, AX.dtype)
+        Ome = D.to_host((Qn.to(dt).conj() @ AX.to(dt)).transpose(0, 1))   # [i, j] = <q_j | O q_i>
+        A_diag = Vn.T.dot(Ome.dot(Vn))
+        res[key] = np.squeeze(np.einsum("j...,l...,jl->...", cc, cc, A_diag))
+    p = np.exp(-np.outer(E[:nv], beta))
+    Id = np.einsum("j,j...->...", Vn[0, :] ** 2, p)
+    return res, np.squeeze(Id)

@@ -9,7 +9,9 @@ What runs from the reference itself:
     expm_multiply_parallel_core.html (text of its <pre> block), with its four
     native wrappers supplied by the oracle restatement (oracle/sparse_oracle.c);
   * scipy.sparse.linalg.expm_multiply, the arbiter of the reference's own
-    tests (test/test_expm_multiply_parallel.py:65-74).
+    tests (test/test_expm_multiply_parallel.py:65-74);
+  * src/quspin/tools/lanczos/_FTLM.py and _LTLM.py, imported unmodified (their
+    import of _get_first_lv resolved to the reference's own _lanczos_utils).
 The basis and Hamiltonian come from the oracle restatement (the reference's
 native basis core is not installable here).
 
@@ -91,6 +93,42 @@ def reference_expm_class():
     return ns["ExpmMultiplyParallel"]
 
 
+def reference_thermal(lz):
+    pkg = types.ModuleType("quspin")
+    tools = types.ModuleType("quspin.tools")
+    lanc = types.ModuleType("quspin.tools.lanczos")
+    sys.modules.update({"quspin": pkg, "quspin.tools": tools, "quspin.tools.lanczos": lanc,
+                        "quspin.tools.lanczos._lanczos_utils": lz})
+    mods = []
+    for name in ("_FTLM", "_LTLM"):
+        path = os.path.join(REF, "src/quspin/tools/lanczos/{}.py".format(name))
+        spec = importlib.util.spec_from_file_location("ref" + name, path)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mods.append(mod)
+    return mods[0].FTLM_static_iteration, mods[1].LTLM_static_iteration
+
+
+def thermal_fixture(lz):
+    """FTLM / LTLM iterations of the reference on an XXZ chain L=14 (k=0,
+    p=+1), operators H and a nearest-neighbour zz correlator."""
+    L = 14
+    m = chain_maps(L)
+    ob = O.OracleBasis(L, [(1, L // 2, 0)], pauli=0, kblock=(m["t"], 0), pblock=(m["p"], 0))
+    H = sp.csr_matrix(O.make_static(ob, xxz_static(L, 1.0, 0.5), np.float64))
+    Czz = sp.csr_matrix(O.make_static(ob, [["zz", [[1.0 / L, i, (i + 1) % L] for i in range(L)]]], np.float64))
+    v0 = np.random.default_rng(7).normal(size=ob.Ns)
+    E, V, Q_T = lz.lanczos_full(H, v0, 40)
+    beta = np.linspace(0.0, 5.0, 11)
+    ftlm, ltlm = reference_thermal(lz)
+    Of, If = ftlm({"H": H, "Czz": Czz}, E, V, Q_T, beta=beta)
+    Ol, Il = ltlm({"H": H, "Czz": Czz}, E, V, Q_T, beta=beta)
+    np.savez_compressed(os.path.join(HERE, "thermal_xxz_L14.npz"), H_indptr=H.indptr, H_indices=H.indices,
+                        H_data=H.data, C_indptr=Czz.indptr, C_indices=Czz.indices, C_data=Czz.data, v0=v0,
+                        E=E, V=V, Q_T=Q_T, beta=beta, ftlm_H=Of["H"], ftlm_C=Of["Czz"], ftlm_I=If,
+                        ltlm_H=Ol["H"], ltlm_C=Ol["Czz"], ltlm_I=Il)
+
+
 def main():
     L = 20
     m = chain_maps(L)
@@ -109,6 +147,7 @@ def main():
     w_scipy = expm_multiply(-1j * H, v)
 
     lz = reference_lanczos()
+    thermal_fixture(lz)
     E, V, Q_T = lz.lanczos_full(H, v0, 60)
     E_iter, V_iter = lz.lanczos_iter(H, v0, 60, return_vec_iter=False)
 

@@ -136,3 +136,22 @@ def test_op_masks_and_pauli_scaling():
     assert np.all(ME0 != 0)
     with pytest.raises(TypeError):
         O.make_static(O.OracleBasis(8, [(1, 4, 0)], pauli=0, kblock=(m["t"], 1)), xxz_static(8), np.float64)
+
+
+def test_oracle_ftlm_ltlm_match_reference_golden():
+    """FTLM / LTLM iterations restated in the oracle equal the reference's
+    own functions (_FTLM.py, _LTLM.py run unmodified by
+    tests/golden/make_golden.py) on the same Lanczos data."""
+    g = np.load(os.path.join(GOLD, "thermal_xxz_L14.npz"))
+    n = g["v0"].size
+    H = sp.csr_matrix((g["H_data"], g["H_indices"], g["H_indptr"]), shape=(n, n))
+    C = sp.csr_matrix((g["C_data"], g["C_indices"], g["C_indptr"]), shape=(n, n))
+    ops = {"H": H, "Czz": C}
+    Of, If = O.ftlm_static_iteration(ops, g["E"], g["V"], g["Q_T"], beta=g["beta"])
+    np.testing.assert_allclose(Of["H"], g["ftlm_H"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(Of["Czz"], g["ftlm_C"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(If, g["ftlm_I"], rtol=1e-12)
+    Ol, Il = O.ltlm_static_iteration(ops, g["E"], g["V"], g["Q_T"], beta=g["beta"])
+    np.testing.assert_allclose(Ol["H"], g["ltlm_H"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(Ol["Czz"], g["ltlm_C"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(Il, g["ltlm_I"], rtol=1e-12)

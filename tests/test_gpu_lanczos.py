@@ -101,3 +101,29 @@ def test_mixed_precision_lanczos(cuda):
     E64 = lanczos_full(H, v0, 60, reorth=True)[0]
     E32 = lanczos_full(H, v0, 60, reorth=True, precision="mixed")[0]
     assert abs(E64[0] - E32[0]) < 1e-6 * max(1.0, abs(E64[0]))
+
+
+def test_ftlm_ltlm_against_reference_golden(cuda):
+    """Device FTLM / LTLM iterations on the reference's own Lanczos data give
+    the reference functions' results (tests/golden/thermal_xxz_L14.npz), with
+    the operators as device matrices and Q_T on the device or as an
+    iterator."""
+    import os
+    import torch
+    import scipy.sparse as sp
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tools import FTLM_static_iteration, LTLM_static_iteration
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "thermal_xxz_L14.npz"))
+    n = g["v0"].size
+    H = sp.csr_matrix((g["H_data"], g["H_indices"], g["H_indptr"]), shape=(n, n))
+    C = sp.csr_matrix((g["C_data"], g["C_indices"], g["C_indptr"]), shape=(n, n))
+    ops = {"H": DeviceCSR.from_scipy(H), "Czz": DeviceCSR.from_scipy(C)}
+    Q = torch.tensor(g["Q_T"], device="cuda")
+    Of, If = FTLM_static_iteration(ops, g["E"], g["V"], Q, beta=g["beta"])
+    np.testing.assert_allclose(Of["H"], g["ftlm_H"], rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(Of["Czz"], g["ftlm_C"], rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(If, g["ftlm_I"], rtol=1e-12)
+    Ol, Il = LTLM_static_iteration(ops, g["E"], g["V"], iter(list(Q)), beta=g["beta"])
+    np.testing.assert_allclose(Ol["H"], g["ltlm_H"], rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(Ol["Czz"], g["ltlm_C"], rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(Il, g["ltlm_I"], rtol=1e-12)
