@@ -165,6 +165,10 @@ int qs_rk_combine(int64_t n2, const double *d_y, const double *d_K, int nk, cons
 int qs_rk_error(int64_t n2, const double *d_y0, const double *d_y1, const double *d_K, int nk,
                 const double *e5_host, const double *e3_host, double atol, double rtol, double *d_scratch,
                 double *d_out, void *stream);
+/* Liouville right-hand side helper (hamiltonian_core.py:1394-1420): out = alpha X^dagger or out += alpha
+ * X^dagger for complex128 n x n matrices (C order; out must not alias X). */
+int qs_adjoint_axpy(int64_t n, const void *d_X, void *d_out, double alpha_re, double alpha_im, int accumulate,
+                    void *stream);
 
 /* ---- many sectors in one launch: block-diagonal stack of sector matrices,
  * per-sector shift / factor / stopping test, common (s, m*) schedule.  The

@@ -73,6 +73,7 @@ _SIGS = {
     "qs_split_pairs": (_i, [_i64, _vp, _vp, _vp]),
     "qs_rk_error_scratch_doubles": (_i, [_i64]),
     "qs_rk_combine": (_i, [_i64, _vp, _vp, _i, _vp, _d, _vp, _vp]),
+    "qs_adjoint_axpy": (_i, [_i64, _vp, _vp, _d, _d, _i, _vp]),
     "qs_rk_error": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "qs_taylor_term": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _d, _d, _vp, _i, _d, _vp,
                             _i, _vp]),

@@ -126,3 +126,53 @@ extern "C" int qs_rk_error(int64_t n2, const double *y0, const double *y1, const
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Adjoint helpers of the Liouville right-hand side -i (H rho - rho H), with
+// rho H = (H^dagger rho^dagger)^dagger (hamiltonian_core.py:1394-1420 builds
+// the same commutator from transposed products).  Square complex128 n x n
+// matrices in C order; 32 x 32 tiles through shared memory so both the read
+// and the write are coalesced.
+
+namespace {
+
+__global__ void adjoint_kernel(int64_t n, const cdbl *__restrict__ X, cdbl *__restrict__ out, cdbl alpha, int accumulate)
+{
+    __shared__ cdbl tile[32][33];
+    const int64_t bi = (int64_t)blockIdx.y * 32, bj = (int64_t)blockIdx.x * 32;
+    // load X[bi + ty + k, bj + tx]
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int64_t r = bi + k, c = bj + threadIdx.x;
+        if (r < n && c < n) tile[k][threadIdx.x] = X[r * n + c];
+    }
+    __syncthreads();
+    // out[bj + ty + k, bi + tx] (+)= alpha conj(X[bi + tx, bj + ty + k])
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int64_t r = bj + k, c = bi + threadIdx.x;
+        if (r < n && c < n) {
+            const cdbl x = tile[threadIdx.x][k];
+            const cdbl v{alpha.x * x.x + alpha.y * x.y, alpha.y * x.x - alpha.x * x.y};   // alpha * conj(x)
+            cdbl *o = out + r * n + c;
+            if (accumulate) { o->x += v.x; o->y += v.y; }
+            else *o = v;
+        }
+    }
+}
+
+}  // namespace
+
+// out = alpha X^dagger (accumulate = 0) or out += alpha X^dagger (accumulate
+// = 1) for complex128 n x n matrices; out must not alias X.
+extern "C" int qs_adjoint_axpy(int64_t n, const void *X, void *out, double alpha_re, double alpha_im, int accumulate,
+                               void *stream)
+{
+    if (n < 0 || (n > 0 && (!X || !out)) || X == out) return QS_ERR_ARG;
+    if (n == 0) return QS_OK;
+    const int64_t t = (n + 31) / 32;
+    if (t > 65535) return QS_ERR_UNSUPPORTED;
+    dim3 grid((unsigned)t, (unsigned)t), block(32, 8);
+    adjoint_kernel<<<grid, block, 0, qs_stream(stream)>>>(n, (const cdbl *)X, (cdbl *)out, cdbl{alpha_re, alpha_im},
+                                                         accumulate);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}

@@ -23,7 +23,10 @@ otherwise.  Here the same method runs with the state resident on the GPU:
 
 Outputs follow the reference: an array of shape (Ns, len(times)) (or
 (Ns, k, len(times))), a generator with ``iterate=True``, imaginary-time states
-renormalised to the initial norm.
+renormalised to the initial norm.  ``eom="LvNE"`` evolves a density matrix
+with d rho / dt = -i [H(t), rho]; the commutator's right product comes from
+the conjugate-transposed parts, rho H = (H^dagger rho^dagger)^dagger, with the
+adjoints taken by a tiled transpose kernel (csrc/ode.cu).
 """
 from __future__ import annotations
 
@@ -174,11 +177,46 @@ class DeviceDOP853:
             h = hnew
 
 
+def _dagger(M):
+    """Device conjugate transpose of a static or dynamic part."""
+    from ..sparse import DeviceCSR, DeviceDIA
+    if isinstance(M, DeviceCSR):
+        return M.conj_transpose()
+    if isinstance(M, DeviceDIA) and bool((M.offsets == 0).all()):
+        return DeviceDIA(M.offsets, M.data.conj().resolve_conj() if M.data.is_complex() else M.data, M.shape,
+                         M.dtype)
+    return DeviceCSR.from_scipy(M.tocsr().conj().T.tocsr(), M.dtype)
+
+
+def _liouville_rhs(H):
+    """rhs(t, rho, out): out = -i (H(t) rho - rho H(t)) with rho H =
+    (H(t)^dagger rho^dagger)^dagger (hamiltonian_core.py:1394-1420)."""
+    parts = [(None, _dagger(H._static))] + [(fn, _dagger(M)) for fn, M in H._dynamic.items()]
+    buf = {}
+
+    def rhs(t, rho, out):
+        n = rho.shape[0]
+        if "rd" not in buf:
+            buf["rd"] = torch.empty_like(rho)
+            buf["y"] = torch.empty_like(rho)
+        rd, y = buf["rd"], buf["y"]
+        H.dot(rho, time=t, out=out, a=-1j)                                   # -i H rho
+        _lib.call("qs_adjoint_axpy", n, D.ptr(rho), D.ptr(rd), 1.0, 0.0, 0, D.stream())   # rho^dagger
+        for k, (fn, Md) in enumerate(parts):
+            c = 1.0 if fn is None else complex(np.conj(fn(t)))
+            Md.matvec_into(rd, y, a=c, overwrite=(k == 0))                    # H^dagger rho^dagger
+        _lib.call("qs_adjoint_axpy", n, D.ptr(y), D.ptr(out), 0.0, 1.0, 1, D.stream())     # += i (..)^dagger
+    return rhs
+
+
 def evolve_hamiltonian(H, v0, t0, times, eom="SE", solver_name="dop853", stack_state=False, verbose=False,
                        iterate=False, imag_time=False, **solver_args):
     """hamiltonian.evolve on the device (see the module docstring)."""
+    if eom == "LvNE":
+        return _evolve_lvne(H, v0, t0, times, solver_name, stack_state, verbose, iterate, imag_time,
+                            **solver_args)
     if eom != "SE":
-        raise NotImplementedError("only eom='SE' (Schroedinger evolution) is implemented on the GPU")
+        raise ValueError("'{} equation' not recognized, must be 'SE' or 'LvNE'".format(eom))
     if solver_name not in ("dop853",):
         raise NotImplementedError("the GPU integrator is DOP853 (solver_name='dop853')")
     if imag_time and stack_state:
@@ -233,3 +271,46 @@ def evolve_hamiltonian(H, v0, t0, times, eom="SE", solver_name="dop853", stack_s
         return v.transpose() if v.ndim == 2 else v.transpose((1, 2, 0))
     v = torch.stack(outs, dim=0)
     return v.permute(1, 0) if v.dim() == 2 else v.permute(1, 2, 0)
+
+
+def _evolve_lvne(H, rho0, t0, times, solver_name, stack_state, verbose, iterate, imag_time, **solver_args):
+    """Liouville - von Neumann evolution d rho / dt = -i [H(t), rho] of a
+    density matrix (hamiltonian_core.py:1598-1617 checks and right-hand side
+    :1394-1420), integrated by the device DOP853 over the n^2 complex entries."""
+    if solver_name not in ("dop853",):
+        raise NotImplementedError("the GPU integrator is DOP853 (solver_name='dop853')")
+    if imag_time:
+        raise NotImplementedError("imaginary time not implemented for Liouville-von Neumann dynamics")
+    if stack_state:
+        raise NotImplementedError("stack_state not implemented for Liouville-von Neumann dynamics")
+    host = not D.is_device_array(rho0)
+    r0 = np.asanyarray(rho0) if host else rho0
+    if r0.ndim != 2:
+        raise ValueError("v0 must have ndim = 2")
+    if tuple(r0.shape) != tuple(H._shape):
+        raise ValueError("v0 must be same shape as Hamiltonian")
+    y0 = (D.to_device(r0, np.complex128) if host else r0.to(torch.complex128)).contiguous().clone()
+    rtol = solver_args.pop("rtol", None)
+    atol = solver_args.pop("atol", None)
+    solver = DeviceDOP853(_liouville_rhs(H), y0, t0, rtol=1e-9 if rtol is None else rtol,
+                          atol=1e-9 if atol is None else atol, nsteps=solver_args.pop("nsteps", None),
+                          max_step=solver_args.pop("max_step", 0.0), first_step=solver_args.pop("first_step", 0.0))
+
+    def fmt(y):
+        out = y.clone()
+        if verbose:
+            print("evolved to time {0}, trace of state {1}".format(solver.t, complex(torch.diagonal(out).sum())))
+        return D.to_host(out) if host else out
+
+    if np.isscalar(times):
+        return fmt(solver.integrate(times))
+
+    def gen():
+        for t in times:
+            yield fmt(solver.integrate(t))
+    if iterate:
+        return gen()
+    outs = [fmt(solver.integrate(t)) for t in times]
+    if host:
+        return np.stack(outs, axis=0).transpose((1, 2, 0))
+    return torch.stack(outs, dim=0).permute(1, 2, 0)

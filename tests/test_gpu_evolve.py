@@ -106,3 +106,43 @@ def test_iterate_and_device_state(cuda):
     assert np.abs(w.cpu().numpy() - outs[1]).max() < 1e-9
     with pytest.raises(ValueError):
         H.evolve(v0[:-1], 0.0, [1.0])
+
+
+def test_liouville_evolution(cuda):
+    """eom='LvNE': rho(t) = U rho0 U^dagger for a static H (dense exponential on
+    a small sector) and the commutator equation integrated by scipy's ode for a
+    driven H (the reference's own route, hamiltonian_core.py:1394-1420)."""
+    from scipy.linalg import expm
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    L = 10
+    m = chain_maps(L)
+    b = spin_basis_general(L, Nup=L // 2, kblock=(m["t"], 1), pauli=0)
+    H = hamiltonian(xxz_static(L), [], basis=b, dtype=np.complex128)
+    A = H.toarray() if hasattr(H, "toarray") else H.tocsr().toarray()
+    n = A.shape[0]
+    rng = np.random.default_rng(8)
+    X = rng.normal(size=(n, 3)) + 1j * rng.normal(size=(n, 3))
+    rho0 = X @ np.diag([0.5, 0.3, 0.2]) @ X.conj().T
+    rho0 /= np.trace(rho0)
+    times = [0.0, 0.4, 1.1]
+    rt = H.evolve(rho0, 0.0, times, eom="LvNE", rtol=1e-11, atol=1e-11)
+    assert rt.shape == (n, n, len(times))
+    for k, t in enumerate(times):
+        U = expm(-1j * t * A)
+        assert np.abs(rt[:, :, k] - U @ rho0 @ U.conj().T).max() < 1e-9
+    drive = lambda t, w: np.sin(w * t)
+    Hd = hamiltonian(xxz_static(L), [["zz", [[0.4, i, (i + 1) % L] for i in range(L)], drive, (1.5,)]],
+                     basis=b, dtype=np.complex128)
+    A0 = A
+    A1 = Hd.tocsr(time=np.pi / 3.0).toarray() - A0
+    A1 = A1 / drive(np.pi / 3.0, 1.5)
+
+    def f(t, y):
+        R = y.reshape(n, n)
+        Ht = A0 + drive(t, 1.5) * A1
+        return (-1j * (Ht @ R - R @ Ht)).reshape(-1)
+    ref = _scipy_dop853(f, rho0.reshape(-1), 0.0, [0.0, 0.9], 1e-11, 1e-11)
+    got = Hd.evolve(rho0, 0.0, [0.0, 0.9], eom="LvNE", rtol=1e-11, atol=1e-11)
+    assert np.abs(got[:, :, 1] - ref[:, 1].reshape(n, n)).max() < 1e-8
+    with pytest.raises(NotImplementedError):
+        H.evolve(rho0, 0.0, [1.0], eom="LvNE", imag_time=True)
