@@ -1,9 +1,10 @@
 """GPU tools of the hot path: expm_multiply_parallel, Lanczos, matvec."""
 from .batched import MultiSectorExpm
+from .floquet import Floquet
 from .expm_multiply_parallel import ExpmMultiplyParallel, expm_multiply_parallel
 from .lanczos import (FTLM_static_iteration, LTLM_static_iteration, expm_lanczos, lanczos_full, lanczos_iter,
                       lin_comb_Q_T)
 from .matvec import get_matvec_function, matvec
 
-__all__ = ["FTLM_static_iteration", "LTLM_static_iteration", "ExpmMultiplyParallel", "expm_multiply_parallel", "lanczos_full", "lanczos_iter", "lin_comb_Q_T",
+__all__ = ["Floquet", "FTLM_static_iteration", "LTLM_static_iteration", "ExpmMultiplyParallel", "expm_multiply_parallel", "lanczos_full", "lanczos_iter", "lin_comb_Q_T",
            "expm_lanczos", "matvec", "get_matvec_function", "MultiSectorExpm"]
