@@ -81,6 +81,28 @@ def zeros(shape, dtype):
     return torch.zeros(shape, dtype=torch_dtype(dtype), device=device())
 
 
+# Host arrays at least this large cross PCIe / C2C through a page-locked
+# staging buffer (page-locked copies run at the link rate; pageable ones are
+# staged by the driver in small pieces).
+_STAGE_MIN_BYTES = 1 << 20
+_stage = {}
+
+
+def _staging(nbytes):
+    buf = _stage.get("buf")
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(nbytes, _STAGE_MIN_BYTES), dtype=torch.uint8, pin_memory=True)
+        _stage["buf"] = buf
+    return buf[:nbytes]
+
+
+def _pinned(arr):
+    try:
+        return torch.from_numpy(arr).is_pinned()
+    except (TypeError, RuntimeError):
+        return False
+
+
 def to_device(a, dtype=None):
     """Contiguous device tensor from a numpy array / torch tensor / scalar list."""
     if isinstance(a, torch.Tensor):
@@ -97,11 +119,26 @@ def to_device(a, dtype=None):
         arr = arr.view(np.int32)
     elif arr.dtype == np.uint64:
         arr = arr.view(np.int64)
-    return torch.from_numpy(np.ascontiguousarray(arr)).to(device())
+    arr = np.ascontiguousarray(arr)
+    if arr.nbytes < _STAGE_MIN_BYTES or arr.dtype.kind not in "iufc" or _pinned(arr):
+        return torch.from_numpy(arr).to(device())
+    st = _staging(arr.nbytes)
+    st.numpy()[...] = arr.reshape(-1).view(np.uint8)
+    out = torch.empty(arr.shape, dtype=torch_dtype(arr.dtype), device=device())
+    out.view(-1).view(torch.uint8).copy_(st)           # synchronous: the staging buffer is free afterwards
+    return out
 
 
 def to_host(t, dtype=None):
-    arr = t.detach().cpu().numpy()
+    t = t.detach()
+    nbytes = t.numel() * t.element_size()
+    if t.is_cuda and nbytes >= _STAGE_MIN_BYTES and t.dtype in _TORCH_TO_NP:
+        tc = t.contiguous()
+        st = _staging(nbytes)
+        st.copy_(tc.view(-1).view(torch.uint8))            # page-locked device-to-host copy
+        arr = st.numpy().view(np_dtype(tc.dtype)).reshape(tuple(tc.shape)).copy()
+    else:
+        arr = t.cpu().numpy()
     if dtype is not None and arr.dtype != np.dtype(dtype):
         arr = arr.view(dtype) if arr.dtype.itemsize == np.dtype(dtype).itemsize and \
             arr.dtype.kind in "iu" and np.dtype(dtype).kind in "iu" else arr.astype(dtype)
