@@ -105,3 +105,52 @@ def test_hamiltonian_dot_default_form(cuda):
         set_spmv_precision(old)
     assert _rel(w, wi) <= 1e-13
     assert _rel(w, H.tocsr() @ v) <= 1e-13
+
+
+def test_int64_indptr_paths_match_int32(cuda):
+    """Matrices past 2^31 nonzeros carry an int64 indptr (src/quspin/basis/
+    base.py:7-11 picks the index dtype by size); the int64 kernels give the
+    same bits as the int32 ones on a small matrix stored both ways."""
+    import torch
+    from quspin_gb300 import _device as D
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    n = 40000
+    A = _mat(n, True, 9)
+    A = sp.csr_matrix((A + A.conj().T) * 0.05)
+    M32 = DeviceCSR.from_scipy(A)
+    M64 = DeviceCSR(M32.indptr.to(torch.int64), M32.indices, M32.data, M32.shape, M32.dtype)
+    assert M64.idx64 == 1 and M32.idx64 == 0
+    rng = np.random.default_rng(10)
+    x = D.to_device(rng.normal(size=n) + 1j * rng.normal(size=n), np.complex128)
+    for prec in ("double", "ieee"):
+        y32, y64 = torch.empty_like(x), torch.empty_like(x)
+        M32.matvec_into(x, y32, precision=prec, group=0)
+        M64.matvec_into(x, y64, precision=prec, group=0)
+        assert torch.equal(y32, y64), prec
+    for prec in ("double", "ieee", "mixed"):
+        np.random.seed(0)
+        w32 = ExpmMultiplyParallel(M32, a=-0.6j, precision=prec)
+        np.random.seed(0)
+        w64 = ExpmMultiplyParallel(M64, a=-0.6j, precision=prec)
+        w64.set_partition(w32.m_star, w32.s)
+        F32, F64 = x.clone(), x.clone()
+        w32.run_device(F32)
+        w64.run_device(F64)
+        assert torch.linalg.vector_norm(F32 - F64) <= 1e-14 * torch.linalg.vector_norm(F32), prec
+
+
+def test_empty_and_tiny_operators(cuda):
+    """n = 0 and n = 1 operators through the product and the exponential."""
+    import torch
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    A1 = sp.csr_matrix(np.array([[2.0]]))
+    w = ExpmMultiplyParallel(A1, a=-1j).dot(np.array([1.0 + 0j]))
+    assert abs(w[0] - np.exp(-2j)) < 1e-14
+    A0 = sp.csr_matrix((0, 0))
+    M0 = DeviceCSR.from_scipy(A0)
+    x0 = torch.zeros(0, dtype=torch.complex128, device="cuda")
+    y0 = torch.empty_like(x0)
+    M0.matvec_into(x0, y0)
+    assert ExpmMultiplyParallel(A0, a=-1j).dot(np.zeros(0, np.complex128)).shape == (0,)
