@@ -153,6 +153,18 @@ int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, co
                      const void *d_data, int dtype, void *d_F, int64_t nvec, int s, int m_star, double tol,
                      double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
                      void *d_work, int btype, void *d_ctl, int group, void *stream);
+/* The same two calls with a row-sum scratch d_rownorm of n float pairs (8n bytes): with bit 16 of group set and
+ * more than 8 right-hand sides, the float forms sweep the rows once per chunk of 8 vectors, so the gathered
+ * slice of B stays in L2 (the many-state evolutions of hamiltonian_core.py:1472-1486 and block_tools.py:618-795
+ * call the Taylor loop with such blocks). */
+int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                        const void *d_data, int dtype, const void *d_Bin, void *d_Bout, int btype, void *d_F,
+                        int64_t nvec, double mu_re, double mu_im, const void *d_coeff, int j, double tol, void *d_ctl,
+                        int group, void *d_rownorm, void *stream);
+int qs_expm_multiply_rows(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
+                          const void *d_data, int dtype, void *d_F, int64_t nvec, int s, int m_star, double tol,
+                          double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
+                          void *d_work, int btype, void *d_ctl, int group, void *d_rownorm, void *stream);
 
 /* ---- Runge-Kutta stage arithmetic of hamiltonian.evolve: replaces the
  * state updates of scipy's DOP853 that the reference drives through
@@ -180,6 +192,10 @@ int qs_taylor_multi_term(int64_t n, const void *d_indptr, const int32_t *d_indic
                          const void *d_Bin, void *d_Bout, int btype, void *d_F, int64_t nvec, const int64_t *d_sec_off,
                          const void *d_mu, const void *d_coeff, int j, double tol, void *d_ctl, int group,
                          void *stream);
+int qs_taylor_multi_term_rows(int64_t n, const void *d_indptr, const int32_t *d_indices, const void *d_data, int dtype,
+                              const void *d_Bin, void *d_Bout, int btype, void *d_F, int64_t nvec,
+                              const int64_t *d_sec_off, const void *d_mu, const void *d_coeff, int j, double tol,
+                              void *d_ctl, int group, void *d_rownorm, void *stream);
 int qs_taylor_multi_rescale(int64_t n, int64_t nvec, void *d_F, void *d_B0, int btype, const int64_t *d_sec_off,
                             const void *d_eta, int use_eta, void *d_ctl, void *stream);
 

@@ -77,9 +77,13 @@ _SIGS = {
     "qs_rk_error": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "qs_taylor_term": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _d, _d, _vp, _i, _d, _vp,
                             _i, _vp]),
+    "qs_taylor_term_rows": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _d, _d, _vp, _i, _d, _vp,
+                            _i, _vp, _vp]),
     "qs_taylor_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp]),
     "qs_expm_multiply": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i64, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp,
                               _i, _vp, _i, _vp]),
+    "qs_expm_multiply_rows": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i64, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp,
+                              _i, _vp, _i, _vp, _vp]),
     "qs_expm_noalloc_max_elems": (_i64, []),
     "qs_expm_multiply_noalloc": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i64, _i, _i, _d, _d, _d, _d, _d,
                                       _i, _vp]),
@@ -87,6 +91,8 @@ _SIGS = {
     "qs_max_sectors": (_i, []),
     "qs_taylor_multi_term": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _vp, _vp, _vp, _i, _d, _vp, _i,
                                   _vp]),
+    "qs_taylor_multi_term_rows": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, _vp, _vp, _vp, _i, _d, _vp, _i,
+                                       _vp, _vp]),
     "qs_taylor_multi_rescale": (_i, [_i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp]),
     "qs_mlp_dense_fwd": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "qs_mlp_dense_bwd": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

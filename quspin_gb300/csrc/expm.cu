@@ -290,12 +290,31 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // QS_CPF, values split by qs_split_pairs) or QS_C64 (dtype QS_F32 / QS_C64);
 // F is complex128 [n, nvec]; coeff: device complex128 table, term j uses coeff[j];
 // ctl: device control block (qs_expm_ctl_bytes()).  group: launch shape,
-// G | (U << 8) (G lanes per row 2..32, U = 1, 2, 4 entries in flight per lane);
+// G | (U << 8) | (C << 16) (G lanes per row 2..32, U = 1, 2, 4 entries in flight
+// per lane; C = 1 asks the float forms for the chunk-outer sweep, which takes
+// effect only through qs_taylor_term_rows with a row-sum scratch);
 // 0 picks G from nnz/n and U = 2.
+extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
+                                   const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
+                                   int64_t nvec, double mu_re, double mu_im, const void *coeff, int j, double tol,
+                                   void *ctl, int group, void *rownorm, void *stream);
+
 extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                               const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
                               int64_t nvec, double mu_re, double mu_im, const void *coeff, int j, double tol,
                               void *ctl, int group, void *stream)
+{
+    return qs_taylor_term_rows(n, nnz, indptr, idx64, indices, data, dtype, Bin, Bout, btype, F, nvec, mu_re, mu_im,
+                               coeff, j, tol, ctl, group, nullptr, stream);
+}
+
+// qs_taylor_term with row-sum scratch: with rownorm (n float pairs) and the
+// chunk bit of group set (1 << 16), the float forms sweep the rows once per
+// vector chunk of 8 so the gathered slice of B can stay in L2.
+extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
+                                   const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
+                                   int64_t nvec, double mu_re, double mu_im, const void *coeff, int j, double tol,
+                                   void *ctl, int group, void *rownorm, void *stream)
 {
     if (n < 1 || nvec < 1 || !indptr || !Bin || !Bout || !F || !coeff || !ctl || j < 0) return QS_ERR_ARG;
     int G = group > 0 ? (group & 0xff) : pick_group_e(n, nnz);
@@ -309,8 +328,9 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
     const cdbl *cf = reinterpret_cast<const cdbl *>(coeff);
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
     if (lp_btype(btype)) {
+        const int co = group > 0 && ((group >> 16) & 1) && rownorm != nullptr;
         LpTerm a{n, indptr, idx64, indices, data, dtype, Bin, Bout, btype, Fp, nvec, mu, nullptr, nullptr, cf, j, tol,
-                 ctl, G, U, st};
+                 ctl, G, U, co, rownorm, st};
         return lp_taylor_term(a, false);
     }
     if (btype == QS_C128) {
@@ -350,10 +370,27 @@ extern "C" int qs_taylor_rescale(int64_t n, int64_t nvec, void *F, void *B0, int
 // device complex128[max(m_star,1)] with coeff[j] = a / (s (j+1)); eta: device
 // complex128 = exp(a mu / s); one: device complex128 = 1.  ctl zeroed by the
 // caller before the first call.  No host synchronisation.
+extern "C" int qs_expm_multiply_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
+                                     const void *data, int dtype, void *F, int64_t nvec, int s, int m_star,
+                                     double tol, double mu_re, double mu_im, const void *coeff, const void *eta,
+                                     const void *one, void *work, int btype, void *ctl, int group, void *rownorm,
+                                     void *stream);
+
 extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                                 const void *data, int dtype, void *F, int64_t nvec, int s, int m_star, double tol,
                                 double mu_re, double mu_im, const void *coeff, const void *eta, const void *one,
                                 void *work, int btype, void *ctl, int group, void *stream)
+{
+    return qs_expm_multiply_rows(n, nnz, indptr, idx64, indices, data, dtype, F, nvec, s, m_star, tol, mu_re, mu_im,
+                                 coeff, eta, one, work, btype, ctl, group, nullptr, stream);
+}
+
+// qs_expm_multiply with the row-sum scratch of qs_taylor_term_rows.
+extern "C" int qs_expm_multiply_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
+                                     const void *data, int dtype, void *F, int64_t nvec, int s, int m_star,
+                                     double tol, double mu_re, double mu_im, const void *coeff, const void *eta,
+                                     const void *one, void *work, int btype, void *ctl, int group, void *rownorm,
+                                     void *stream)
 {
     if (n < 1 || nvec < 1 || s < 1 || m_star < 0 || !work || !ctl) return QS_ERR_ARG;
     if (btype != QS_C128 && btype != QS_C64 && btype != QS_CPF) return QS_ERR_ARG;
@@ -366,8 +403,8 @@ extern "C" int qs_expm_multiply(int64_t n, int64_t nnz, const void *indptr, int 
         for (int j = 0; j < m_star; j++) {
             void *bin = (j & 1) ? b1 : b0;
             void *bout = (j & 1) ? b0 : b1;
-            rc = qs_taylor_term(n, nnz, indptr, idx64, indices, data, dtype, bin, bout, btype, F, nvec, mu_re, mu_im,
-                                coeff, j, tol, ctl, group, stream);
+            rc = qs_taylor_term_rows(n, nnz, indptr, idx64, indices, data, dtype, bin, bout, btype, F, nvec, mu_re,
+                                     mu_im, coeff, j, tol, ctl, group, rownorm, stream);
             if (rc) return rc;
         }
         rc = qs_taylor_rescale(n, nvec, F, b0, btype, eta, ctl, m_star > 0 ? 1 : 0, stream);
@@ -584,10 +621,25 @@ static int multi_nb(int64_t n, const void *indptr, const int32_t *indices, const
 // coeff: device complex128 table; ctl: MultiCtl (qs_multi_ctl_bytes()) with
 // nsec set.  btype / dtype pairs as for qs_taylor_term.  group as for
 // qs_taylor_term.
+extern "C" int qs_taylor_multi_term_rows(int64_t n, const void *indptr, const int32_t *indices, const void *data,
+                                         int dtype, const void *Bin, void *Bout, int btype, void *F, int64_t nvec,
+                                         const int64_t *sec_off, const void *mu, const void *coeff, int j, double tol,
+                                         void *ctl, int group, void *rownorm, void *stream);
+
 extern "C" int qs_taylor_multi_term(int64_t n, const void *indptr, const int32_t *indices, const void *data, int dtype,
                                     const void *Bin, void *Bout, int btype, void *F, int64_t nvec,
                                     const int64_t *sec_off, const void *mu, const void *coeff, int j, double tol,
                                     void *ctl, int group, void *stream)
+{
+    return qs_taylor_multi_term_rows(n, indptr, indices, data, dtype, Bin, Bout, btype, F, nvec, sec_off, mu, coeff, j,
+                                     tol, ctl, group, nullptr, stream);
+}
+
+// qs_taylor_multi_term with the row-sum scratch of qs_taylor_term_rows.
+extern "C" int qs_taylor_multi_term_rows(int64_t n, const void *indptr, const int32_t *indices, const void *data,
+                                         int dtype, const void *Bin, void *Bout, int btype, void *F, int64_t nvec,
+                                         const int64_t *sec_off, const void *mu, const void *coeff, int j, double tol,
+                                         void *ctl, int group, void *rownorm, void *stream)
 {
     if (n < 1 || nvec < 1 || !indptr || !Bin || !Bout || !F || !sec_off || !mu || !coeff || !ctl || j < 0)
         return QS_ERR_ARG;
@@ -600,8 +652,9 @@ extern "C" int qs_taylor_multi_term(int64_t n, const void *indptr, const int32_t
     const cdbl *cf = reinterpret_cast<const cdbl *>(coeff);
     cdbl *Fp = reinterpret_cast<cdbl *>(F);
     if (lp_btype(btype)) {
+        const int co = group > 0 && ((group >> 16) & 1) && rownorm != nullptr;
         LpTerm a{n, indptr, 0, indices, data, dtype, Bin, Bout, btype, Fp, nvec, cdbl{0.0, 0.0}, m, sec_off, cf, j, tol,
-                 ctl, G, U, st};
+                 ctl, G, U, co, rownorm, st};
         return lp_taylor_term(a, true);
     }
     if (btype == QS_C128) {

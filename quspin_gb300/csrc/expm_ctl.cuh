@@ -117,6 +117,8 @@ struct LpTerm {
     double tol;
     void *ctl;
     int G, U;
+    int chunk_outer;          // sweep rows once per NB-wide vector chunk (needs rownorm)
+    void *rownorm;            // n float pairs of row-sum scratch for chunk_outer, or null
     cudaStream_t st;
 };
 

@@ -41,7 +41,8 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                                                         typename M::BE *__restrict__ Bout, cdbl *__restrict__ F,
                                                         int64_t nvec, cdbl mu0, const cdbl *__restrict__ mus,
                                                         const int64_t *__restrict__ sec_off,
-                                                        const cdbl *__restrict__ coeff, int j, double tol, void *ctlp)
+                                                        const cdbl *__restrict__ coeff, int j, double tol, void *ctlp,
+                                                        float2 *__restrict__ rownorm)
 {
     using S = typename M::S;
     using BE = typename M::BE;
@@ -99,9 +100,20 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
     const S cf_re = s_cf[0];
     const S cf_x = comp ? s_cf[1] : M::neg(s_cf[1]);
     float mb = 0.f, mf = 0.f;
+    // Chunk-outer order (rownorm given, several NB-wide vector chunks): the
+    // whole grid sweeps the rows once per chunk, so the gathered slice of B
+    // is NB columns wide and can stay in L2 across the sweep; the row sums
+    // of the stopping test are carried between sweeps in rownorm (the same
+    // thread owns the same rows in every sweep).
+    const int64_t nchunk = (nvec + NB - 1) / NB;
+    const bool chunk_outer = rownorm != nullptr && nchunk > 1;
+    const int64_t sweeps = chunk_outer ? nchunk : 1;
+    const int64_t r_hi = n;
+    for (int64_t sw = 0; sw < sweeps; sw++) {
+    const int64_t c_begin = chunk_outer ? sw * NB : 0;
+    const int64_t c_end = chunk_outer ? (c_begin + NB < nvec ? c_begin + NB : nvec) : nvec;
     // Rows are handed out per warp (GPW consecutive rows per warp and
     // iteration), so every lane reaches the full-mask shuffles.
-    const int64_t r_hi = n;
     for (int64_t rb = warp * GPW; rb < r_hi; rb += nwarps * GPW) {
         const int64_t r = rb + gsub;
         int sec = 0;
@@ -119,7 +131,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
             bo_pre = M::ldB(Bin + r);
             f_pre = __ldcs(reinterpret_cast<const double *>(F + r) + comp);
         }
-        for (int64_t c0 = 0; c0 < nvec; c0 += NB) {
+        for (int64_t c0 = c_begin; c0 < c_end; c0 += NB) {
             S ar[NB], ai[NB];
 #pragma unroll
             for (int b = 0; b < NB; b++) ar[b] = ai[b] = M::zero();
@@ -182,7 +194,15 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                 }
             }
         }
-        if (writer) {
+        if (chunk_outer && writer && lane == 0) {
+            float2 acc = sw == 0 ? make_float2(0.f, 0.f) : rownorm[r];
+            acc.x += rbn;
+            acc.y += rfn;
+            if (sw + 1 < sweeps) rownorm[r] = acc;
+            rbn = acc.x;
+            rfn = acc.y;
+        }
+        if (writer && sw + 1 == sweeps) {
             if constexpr (MULTI) {
                 if (lane == 0) {
                     atomicMax(&s_mb[sec], __float_as_uint(rbn));
@@ -193,6 +213,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                 mf = fmaxf(mf, rfn);
             }
         }
+    }
     }
 
     if constexpr (!MULTI) {
@@ -249,8 +270,9 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
     int64_t n, int lgG, const IT *__restrict__ indptr, const int32_t *__restrict__ indices,                   \
         const DV *__restrict__ data, const typename M::BE *__restrict__ Bin, typename M::BE *__restrict__ Bout, \
         cdbl *__restrict__ F, int64_t nvec, cdbl mu0, const cdbl *__restrict__ mus,                           \
-        const int64_t *__restrict__ sec_off, const cdbl *__restrict__ coeff, int j, double tol, void *ctlp
-#define TAYLOR_LP_ARGS n, lgG, indptr, indices, data, Bin, Bout, F, nvec, mu0, mus, sec_off, coeff, j, tol, ctlp
+        const int64_t *__restrict__ sec_off, const cdbl *__restrict__ coeff, int j, double tol, void *ctlp, \
+        float2 *__restrict__ rownorm
+#define TAYLOR_LP_ARGS n, lgG, indptr, indices, data, Bin, Bout, F, nvec, mu0, mus, sec_off, coeff, j, tol, ctlp, rownorm
 
 template <class M, class DV, class IT, int NB, int U, bool MULTI>
 __global__ void __launch_bounds__(256) taylor_lp_kernel(TAYLOR_LP_PARAMS)
@@ -379,7 +401,8 @@ int lp_go(const LpTerm &a)
     const int blocks = taylor_grid(a.n, a.G);
     taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
         a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-        (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl);
+        (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl,
+        a.chunk_outer ? (float2 *)a.rownorm : nullptr);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }

@@ -139,10 +139,13 @@ class DrivenEvolution:
         consts = D.to_device(np.concatenate([coeff, [np.exp(a * mu / s), 1.0]]).astype(np.complex128))
         k = max(m, 1)
         op, bt, group = self._operand(M)
-        _lib.call("qs_expm_multiply", self.n, op.nnz, D.ptr(op.indptr), op.idx64, D.ptr(op.indices), D.ptr(op.data),
-                  op.vcode, D.ptr(F), self.nvec, int(s), int(m), float(np.finfo(np.float64).eps / 2),
+        if "_rown" not in self.__dict__:
+            self._rown = torch.empty(2 * self.n, dtype=torch.float32, device=D.device())
+        rown = self._rown if (bt != _lib.C128 and self.nvec > 8) else None
+        _lib.call("qs_expm_multiply_rows", self.n, op.nnz, D.ptr(op.indptr), op.idx64, D.ptr(op.indices),
+                  D.ptr(op.data), op.vcode, D.ptr(F), self.nvec, int(s), int(m), float(np.finfo(np.float64).eps / 2),
                   mu.real, mu.imag, D.ptr(consts[:k]), D.ptr(consts[k:k + 1]), D.ptr(consts[k + 1:]),
-                  D.ptr(self._work), bt, D.ptr(self._ctl), group, D.stream())
+                  D.ptr(self._work), bt, D.ptr(self._ctl), group, D.ptr(rown), D.stream())
         self._keep = consts
 
     def run(self, F, t0, dt, nsteps, mode="plain", predictor=None, segment=50, record=None):

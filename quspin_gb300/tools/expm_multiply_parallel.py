@@ -195,6 +195,14 @@ class ExpmMultiplyParallel:
             self._bufs = {key: b}
         return b
 
+    def _rownorm(self, n):
+        """Row-sum scratch (n float pairs) of the chunk-outer Taylor sweep."""
+        r = self.__dict__.get("_rown")
+        if r is None or r.numel() < 2 * n:
+            r = torch.empty(max(2 * n, 2), dtype=torch.float32, device=D.device())
+            self._rown = r
+        return r
+
     # below this many states x vectors a dot replays a captured launch
     # sequence (one graph launch instead of about s (m* + 2) kernel launches)
     GRAPH_MAX_ELEMS = 1 << 18
@@ -241,9 +249,10 @@ class ExpmMultiplyParallel:
         onep = consts[max(m, 1) + 1:]
         from ..tune import tune_taylor
         group = tune_taylor(M, nvec, btype)
-        _lib.call("qs_expm_multiply", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
+        rown = self._rownorm(n) if (btype != _lib.C128 and nvec > 8) else None
+        _lib.call("qs_expm_multiply_rows", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
                   M.vcode, D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, D.ptr(cf), D.ptr(etap),
-                  D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), group, D.stream())
+                  D.ptr(onep), D.ptr(wbuf), btype, D.ptr(ctl), group, D.ptr(rown), D.stream())
         return consts
 
     def _run_graph(self, F, tol):

@@ -85,13 +85,19 @@ def tune_taylor(M, nvec, btype):
     ctl = torch.zeros(6, dtype=torch.int64, device=D.device())
     coeff = torch.tensor([1e-3 + 0j], dtype=torch.complex128, device=D.device())
     best, best_t = 0, None
-    for G, U in _candidates(n, M.nnz, nvec):
-        code = encode(G, U)
+    cands = [(G, U, 0) for G, U in _candidates(n, M.nnz, nvec)]
+    rown = None
+    if btype != _lib.C128 and nvec > 8:
+        # chunk-outer sweeps (one per 8 vectors) keep the gathered slice of B in L2
+        cands += [(G, U, 1) for G, U, _ in cands]
+        rown = torch.empty(2 * n, dtype=torch.float32, device=D.device())
+    for G, U, ch in cands:
+        code = encode(G, U) | (ch << 16)
 
         def run():
-            _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
+            _lib.call("qs_taylor_term_rows", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data),
                       M.vcode, D.ptr(b0), D.ptr(b1), btype, D.ptr(F), nvec, 0.0, 0.0, D.ptr(coeff), 0, 0.0,
-                      D.ptr(ctl), code, D.stream())
+                      D.ptr(ctl), code, D.ptr(rown), D.stream())
         t = _time(run)
         if best_t is None or t < best_t:
             best, best_t = code, t

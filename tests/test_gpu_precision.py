@@ -123,3 +123,32 @@ def test_multisector_forms(cuda):
         for A, V, W in zip(hosts, blocks, out):
             ref = O.ExpmMultiplyParallelOracle(A, a=-1.5j).dot(V)
             assert _rel(W, ref) <= tol, (p, _rel(W, ref))
+
+
+def test_chunk_outer_sweep_matches_row_order(cuda):
+    """With more than 8 right-hand sides the float forms can sweep the rows
+    once per chunk of 8 vectors (row sums carried in a scratch array); the
+    result equals the one-sweep order to the stopping tolerance."""
+    import torch
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tune import encode
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    rs = np.random.RandomState(11)
+    N = 70000
+    A = sp.random(N, N, density=20.0 / N, format="csr", random_state=rs)
+    A = sp.csr_matrix((A + A.T) * 0.5)
+    V = _state(N, 12, 16)
+    for prec, bt in (("double", _lib.CPF), ("mixed", _lib.C64)):
+        res = []
+        for chunk in (0, 1):
+            op = ExpmMultiplyParallel(DeviceCSR.from_scipy(A), a=-0.5j, precision=prec)
+            M, _ = op._operand()
+            M.__dict__.setdefault("_tuned", {})[("taylor", 16, bt)] = encode(4, 1) | (chunk << 16)
+            F = torch.tensor(V, device="cuda")
+            op.run_device(F)
+            res.append(F.cpu().numpy())
+        assert _rel(res[1], res[0]) <= (1e-13 if prec == "double" else 1e-6), prec
+    np.random.seed(1)
+    wo = O.ExpmMultiplyParallelOracle(A, a=-0.5j).dot(V)
+    assert _rel(res[0], wo) <= 1e-5
