@@ -292,7 +292,8 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // ctl: device control block (qs_expm_ctl_bytes()).  group: launch shape,
 // G | (U << 8) | (C << 16) (G lanes per row 2..32, U = 1, 2, 4 entries in flight
 // per lane; C = 1 asks the float forms for the chunk-outer sweep, which takes
-// effect only through qs_taylor_term_rows with a row-sum scratch);
+// effect only through qs_taylor_term_rows with a row-sum scratch; bit 17
+// narrows its chunks from 8 to 4 vectors);
 // 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                                    const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
@@ -330,7 +331,7 @@ extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, i
     if (lp_btype(btype)) {
         const int co = group > 0 && ((group >> 16) & 1) && rownorm != nullptr;
         LpTerm a{n, indptr, idx64, indices, data, dtype, Bin, Bout, btype, Fp, nvec, mu, nullptr, nullptr, cf, j, tol,
-                 ctl, G, U, co, rownorm, st};
+                 ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
         return lp_taylor_term(a, false);
     }
     if (btype == QS_C128) {
@@ -654,7 +655,7 @@ extern "C" int qs_taylor_multi_term_rows(int64_t n, const void *indptr, const in
     if (lp_btype(btype)) {
         const int co = group > 0 && ((group >> 16) & 1) && rownorm != nullptr;
         LpTerm a{n, indptr, 0, indices, data, dtype, Bin, Bout, btype, Fp, nvec, cdbl{0.0, 0.0}, m, sec_off, cf, j, tol,
-                 ctl, G, U, co, rownorm, st};
+                 ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
         return lp_taylor_term(a, true);
     }
     if (btype == QS_C128) {

@@ -118,6 +118,7 @@ struct LpTerm {
     void *ctl;
     int G, U;
     int chunk_outer;          // sweep rows once per NB-wide vector chunk (needs rownorm)
+    int narrow;               // chunk-outer with 4-vector chunks instead of 8
     void *rownorm;            // n float pairs of row-sum scratch for chunk_outer, or null
     cudaStream_t st;
 };

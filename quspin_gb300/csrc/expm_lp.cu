@@ -418,7 +418,7 @@ int lp_nb(const LpTerm &a)
         return lp_go<M, DV, IT, 1, 1, MULTI>(a);
     }
     if (a.nvec == 2) return lp_go<M, DV, IT, 2, 1, MULTI>(a);
-    if (a.nvec <= 4) return lp_go<M, DV, IT, 4, 1, MULTI>(a);
+    if (a.nvec <= 4 || (a.chunk_outer && a.narrow)) return lp_go<M, DV, IT, 4, 1, MULTI>(a);
     return lp_go<M, DV, IT, 8, 1, MULTI>(a);
 }
 
