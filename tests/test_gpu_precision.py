@@ -134,9 +134,10 @@ def test_chunk_outer_sweep_matches_row_order(cuda):
     from quspin_gb300.sparse import DeviceCSR
     from quspin_gb300.tune import encode
     from quspin_gb300.tools import ExpmMultiplyParallel
-    rs = np.random.RandomState(11)
+    rng = np.random.default_rng(11)
     N = 70000
-    A = sp.random(N, N, density=20.0 / N, format="csr", random_state=rs)
+    r, c = rng.integers(0, N, 20 * N), rng.integers(0, N, 20 * N)
+    A = sp.csr_matrix((rng.uniform(size=20 * N), (r, c)), shape=(N, N))
     A = sp.csr_matrix((A + A.T) * 0.5)
     V = _state(N, 12, 16)
     for prec, bt in (("double", _lib.CPF), ("mixed", _lib.C64)):
