@@ -280,6 +280,14 @@ __global__ void __launch_bounds__(256) taylor_lp_kernel(TAYLOR_LP_PARAMS)
     taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
 }
 
+// The eight-column shapes hold 32 pair accumulators per lane; capping them at
+// three resident blocks per SM keeps 24 warps for the gathers.
+template <class M, class DV, class IT, int NB, int U, bool MULTI>
+__global__ void __launch_bounds__(256, 3) taylor_lp_kernel_wide(TAYLOR_LP_PARAMS)
+{
+    taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
+}
+
 // F = eta F (per sector for MULTI) and the row-norm maximum; the last block
 // sets c1 = ||F||_inf, the storage exponent bexp and clears the per-substep
 // state (counting, at a substep end, a stopping test that never fired).
@@ -399,10 +407,15 @@ int lp_go(const LpTerm &a)
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
     const int blocks = taylor_grid(a.n, a.G);
-    taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
-        a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-        (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl,
-        a.chunk_outer ? (float2 *)a.rownorm : nullptr);
+    float2 *rn = a.chunk_outer ? (float2 *)a.rownorm : nullptr;
+    if constexpr (NB >= 8)
+        taylor_lp_kernel_wide<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
+            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
+    else
+        taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
+            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
