@@ -107,6 +107,24 @@ int qs_inplace_op(void *sym, const void *d_states, const uint32_t *d_norms, int6
                   int conjugated, double a_re, double a_im, const void *d_vin, void *d_vout, int64_t nvec,
                   int *d_err, void *stream);
 
+/* ---- basis.get_proj / project_from / project_to (base_general.py:521-718)
+ * Projector columns (CSC): column i sums c_i chi(g) sigma(g) over the group
+ * elements g reaching each image of representative i, c_i = 1/sqrt(n_i |G|),
+ * rows ascending; images whose unit-phase sum is below 1e-12 are dropped.
+ * mode 0 writes the entry count of column i to d_colptr[i + 1]; mode 1
+ * (d_colptr now offsets) writes rows and complex128 values.  pcon = 0:
+ * row = 2^N - 1 - state (N <= 62); pcon = 1: row = index in the
+ * particle-conserving basis p_states..p_end.  d_err bits: 2 count mismatch,
+ * 4 image outside the row basis.  |G| <= 8192. */
+int qs_proj_fill(void *sym, const void *d_states, const uint32_t *d_norms, int64_t Ns, int gsize, int mode,
+                 int64_t *d_colptr, int pcon, const void *d_p_states, int64_t p_Ns, int p_N_p,
+                 const int64_t *d_p_begin, const int64_t *d_p_end, int64_t *d_rows, void *d_vals, int *d_err,
+                 void *stream);
+/* direction 0: y[Nfull, k] += P x (zero y first; sectors accumulate);
+ * direction 1: y[Ns, k] = P^dagger x.  Complex128, C order. */
+int qs_proj_apply(int direction, int64_t Ns, const int64_t *d_colptr, const int64_t *d_rows, const void *d_P,
+                  const void *d_x, int64_t k, void *d_y, void *stream);
+
 /* ---- _matvec for csr / dia (html matvec/matvec_core.html:146-201) ------- */
 int qs_csr_matvec(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                   const void *d_data, int dtype, const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re,

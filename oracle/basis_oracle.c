@@ -15,6 +15,7 @@
  *   normalization         base_general.py:1119-1181
  *   op (ME,row,col)       base_general.py:292-352
  *   inplace_op            base_general.py:354-410
+ *   orbit (get_proj)      base_general.py:521-582
  *
  * Conventions (documented in sphinx/source/tutorials/user_basis.rst:56-93 and
  * the class docstrings; see the header of oracle/oracle.py for the list):
@@ -413,6 +414,52 @@ int orc_normalization(int N, int fermion, int nmaps, const int32_t *maps,
     #pragma omp parallel for
     for (int64_t i = 0; i < n; i++) out[i] = (uint32_t)orc_check_state(&S, states[i], costab);
     free(costab);
+    orc_sym_free(&S);
+    return 0;
+}
+
+/* Every group element applied to each state, in the odometer order of
+ * orc_ref_state: images[i*G + e], the fermion sign and the phase index of
+ * the element (G = product of the periods).  The projector of get_proj
+ * (base_general.py:521-582) is sum_g chi(g) sign(g) |g s> / sqrt(n |G|)
+ * per representative s; the Python side sums the duplicate images. */
+int orc_orbit(int N, int fermion, int nmaps, const int32_t *maps,
+              const int32_t *pers, const int32_t *qs,
+              const uint64_t *states, int64_t n, int64_t G,
+              uint64_t *images, int8_t *signs, int32_t *phases)
+{
+    orc_sym S;
+    if (orc_sym_init(&S, N, fermion, nmaps, maps, pers, qs)) { orc_sym_free(&S); return -2; }
+    int K = S.nmaps;
+    #pragma omp parallel for
+    for (int64_t i = 0; i < n; i++) {
+        u64 cur[ORC_MAX_MAPS + 1];
+        int sg[ORC_MAX_MAPS + 1], ph[ORC_MAX_MAPS + 1], idx[ORC_MAX_MAPS];
+        for (int d = 0; d <= K; d++) { cur[d] = states[i]; sg[d] = 1; ph[d] = 0; }
+        for (int d = 0; d < K; d++) idx[d] = 0;
+        int64_t e = 0;
+        for (;;) {
+            if (e < G) {
+                images[i * G + e] = cur[K];
+                signs[i * G + e] = (int8_t)sg[K];
+                phases[i * G + e] = ph[K];
+            }
+            e++;
+            int d = K - 1;
+            while (d >= 0) {
+                idx[d]++;
+                if (idx[d] < S.pers[d]) {
+                    cur[d + 1] = orc_map(&S, d, cur[d + 1], &sg[d + 1]);
+                    ph[d + 1] = (ph[d + 1] + S.step[d]) % S.L;
+                    for (int f = d + 1; f < K; f++) { cur[f + 1] = cur[d + 1]; sg[f + 1] = sg[d + 1]; ph[f + 1] = ph[d + 1]; }
+                    break;
+                }
+                idx[d] = 0;
+                d--;
+            }
+            if (d < 0) break;
+        }
+    }
     orc_sym_free(&S);
     return 0;
 }

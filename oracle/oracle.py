@@ -78,6 +78,8 @@ def lib():
             L.orc_representative.restype = c.c_int
             L.orc_normalization.argtypes = sym + [_u64p, c.c_int64, _u32p]
             L.orc_normalization.restype = c.c_int
+            L.orc_orbit.argtypes = sym + [_u64p, c.c_int64, c.c_int64, _u64p, c.c_void_p, _i32p]
+            L.orc_orbit.restype = c.c_int
             opargs = sym + [_f64p, _f64p, c.c_char_p, _i32p, c.c_int, c.c_double, c.c_double,
                             _u64p, _u32p, c.c_int64, c.c_int, _i64p, _i64p]
             L.orc_op.argtypes = opargs + [_i64p, _i64p, _f64p]
@@ -265,6 +267,38 @@ class OracleBasis:
         out = np.zeros(len(s), dtype=np.uint32)
         lib().orc_normalization(*self._symargs(), s, len(s), out)
         return out
+
+    def get_proj(self, dtype, pcon_basis=None):
+        """Restates basis.get_proj (base_general.py:521-582): column i is
+        sum_g chi(g) sign(g) |g s_i> / sqrt(n_i |G|), duplicate images summed
+        (scipy CSC), images whose unit-phase sum is at most 1e-12 dropped.
+        Rows: 2^N - 1 - state, or the index in pcon_basis."""
+        G = int(np.prod(self.pers, dtype=np.int64)) if len(self.pers) else 1
+        n = self.Ns
+        images = np.zeros(n * G, np.uint64)
+        signs = np.zeros(n * G, np.int8)
+        phases = np.zeros(n * G, np.int32)
+        rc = lib().orc_orbit(*self._symargs(), self.states, n, G, images, signs.ctypes.data_as(ctypes.c_void_p),
+                             phases)
+        if rc:
+            raise ValueError("unsupported symmetry map")
+        c = 1.0 / np.sqrt(self.norms.astype(np.float64) * G)
+        unit = (self.phase_re[phases] + 1j * self.phase_im[phases]) * signs
+        cols = np.repeat(np.arange(n), G)
+        if pcon_basis is None:
+            Ns_full = 2 ** self.N
+            rows = (Ns_full - 1) - images.astype(np.int64)
+        else:
+            Ns_full = pcon_basis.Ns
+            rows = pcon_basis.index(images)
+        P = sp.csc_matrix((unit, (rows, cols)), shape=(Ns_full, n))
+        P.sum_duplicates()
+        # images whose summed unit phases cancel (maps that do not commute)
+        P.data[np.abs(P.data) <= 1e-12] = 0.0
+        P.eliminate_zeros()
+        P = sp.csc_matrix(P @ sp.diags(c))
+        dtype = np.dtype(dtype)
+        return P.astype(dtype) if dtype.kind == "c" else sp.csc_matrix(P.real.astype(dtype))
 
     # -- operators -------------------------------------------------------
     def _prep(self, opstr, indx, J):

@@ -60,6 +60,9 @@ _SIGS = {
     "qs_csr_t_fill": (_i, [_i, _i64, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qs_inplace_op": (_i, [_vp, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _vp,
                            _vp, _i64, _vp, _vp]),
+    "qs_proj_fill": (_i, [_vp, _vp, _vp, _i64, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp,
+                          _vp]),
+    "qs_proj_apply": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "qs_csr_matvec": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp]),
     "qs_csr_matvec_pairs": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp, _vp,
                                  _vp]),

@@ -482,6 +482,148 @@ class basis_general:
             return v_out
         return y.squeeze()
 
+    # -- projector to the full / particle-conserving basis -------------------
+    def _pcon_basis(self):
+        """The same particle sector without symmetries (rows of the pcon
+        projector), built once."""
+        b = getattr(self, "_basis_pcon", None)
+        if b is None:
+            b = object.__new__(type(self))
+            b._allowed_ops = getattr(self, "_allowed_ops", set())
+            b._init_general(self._N, self._sectors, blocks=None)
+            b.make()
+            self._basis_pcon = b
+        return b
+
+    def _proj_device(self, pcon=False):
+        """Device CSC of the projector: (colptr int64[Ns+1], rows int64,
+        values complex128, Ns_full).  Built once per row space."""
+        if not self._made_basis:
+            raise AttributeError("this function requires the basis to be constructed first; use basis.make().")
+        pcon = bool(pcon) and len(self._sectors) == 1 and self._sectors[0][0] != 0
+        cache = self.__dict__.setdefault("_proj_cache", {})
+        if pcon in cache:
+            return cache[pcon]
+        gsize = int(np.prod(self._pers, dtype=np.int64)) if len(self._pers) else 1
+        Ns = self._Ns
+        if pcon:
+            pb = self._pcon_basis()
+            Ns_full = pb.Ns
+            pargs = (D.ptr(pb._basis), pb.Ns, pb._N_p, D.ptr(pb._begin), D.ptr(pb._end))
+        else:
+            if self._N > 62:
+                raise NotImplementedError("the full space of more than 62 bits has no int64 index")
+            Ns_full = 2 ** self._N
+            pargs = (None, 0, 0, None, None)
+        colptr = torch.zeros(Ns + 1, dtype=torch.int64, device=D.device())
+        err = D.err_flag()
+        base = (self._sym, D.ptr(self._basis), D.ptr(self._n_dev), Ns, gsize)
+        if Ns:
+            # pass 1: entries per column, then offsets
+            _lib.call("qs_proj_fill", *base, 0, D.ptr(colptr), int(pcon), *pargs, None, None, D.ptr(err),
+                      D.stream())
+            torch.cumsum(colptr[1:].clone(), 0, out=colptr[1:])
+        nnz = int(colptr[-1].item())
+        rows = torch.empty(max(nnz, 1), dtype=torch.int64, device=D.device())
+        vals = torch.empty(max(nnz, 1), dtype=torch.complex128, device=D.device())
+        if Ns:
+            _lib.call("qs_proj_fill", *base, 1, D.ptr(colptr), int(pcon), *pargs, D.ptr(rows), D.ptr(vals),
+                      D.ptr(err), D.stream())
+            e = int(err.item())
+            if e:
+                raise RuntimeError("projector construction failed (error bits {})".format(e))
+        cache[pcon] = (colptr, rows[:nnz], vals[:nnz], Ns_full)
+        return cache[pcon]
+
+    def get_proj(self, dtype, pcon=False):
+        """Projector from the symmetry-reduced to the full basis as a
+        scipy.sparse.csc_matrix (base_general.py:521-582)."""
+        import scipy.sparse as sp
+        colptr, rows, vals, Ns_full = self._proj_device(pcon)
+        dtype = np.dtype(dtype)
+        v = D.to_host(vals)
+        if dtype.kind != "c":
+            if np.any(np.abs(v.imag) > 1.1e-15):
+                raise TypeError("attemping to use real type for complex elements.")
+            v = v.real
+        index_type = np.result_type(np.min_scalar_type(-Ns_full), np.int32)
+        return sp.csc_matrix((v.astype(dtype), D.to_host(rows).astype(index_type),
+                              D.to_host(colptr).astype(index_type)), shape=(Ns_full, self._Ns))
+
+    def _project(self, v0, direction, pcon):
+        colptr, rows, vals, Ns_full = self._proj_device(pcon)
+        host = not D.is_device_array(v0)
+        vdt = np.asarray(v0).dtype if host else D.np_dtype(v0.dtype)
+        squeeze = v0.ndim == 1
+        n_in = self._Ns if direction == 0 else Ns_full
+        n_out = Ns_full if direction == 0 else self._Ns
+        x = D.to_device(v0, np.complex128).reshape(n_in, -1).contiguous()
+        k = x.shape[1]
+        y = torch.zeros((n_out, k), dtype=torch.complex128, device=D.device())
+        if self._Ns and k:
+            _lib.call("qs_proj_apply", direction, self._Ns, D.ptr(colptr), D.ptr(rows), D.ptr(vals), D.ptr(x), k,
+                      D.ptr(y), D.stream())
+        # the reference writes into an array of v0's dtype; a real v0 whose
+        # image is complex (a complex projector) is promoted instead
+        rdt = vdt
+        if vdt.kind != "c":
+            if bool(torch.any(y.imag.abs() > 1.1e-15)):
+                rdt = np.result_type(vdt, np.complex64)
+            else:
+                y = y.real
+        y = y.to(D.torch_dtype(rdt))
+        if squeeze:
+            y = y.reshape(-1)
+        return D.to_host(y) if host else y
+
+    def project_from(self, v0, sparse=True, pcon=False):
+        """State(s) in the symmetry-reduced basis -> full basis, one state
+        per column (base_general.py:696-777)."""
+        import scipy.sparse as sp
+        if not self._made_basis:
+            raise AttributeError("this function requires the basis to be cosntructed first, see basis.make().")
+        if not hasattr(v0, "shape"):
+            v0 = np.asanyarray(v0)
+        if v0.ndim not in (1, 2):
+            raise ValueError("excpecting v0 to have ndim > 0 and at most 2")
+        if v0.shape[0] != self._Ns:
+            raise ValueError("v0 shape {0} not compatible with Ns={1}".format(v0.shape, self._Ns))
+        if sp.issparse(v0):
+            raise ValueError
+        if sparse:
+            vh = D.to_host(v0) if D.is_device_array(v0) else np.ascontiguousarray(v0)
+            if vh.ndim == 1:
+                vh = vh.reshape(-1, 1)
+            return self.get_proj(vh.dtype, pcon=pcon).dot(sp.csc_matrix(vh))
+        return self._project(v0, 0, pcon)
+
+    def get_vec(self, v0, sparse=True, pcon=False):
+        """Deprecated alias of project_from (base_general.py:685-694)."""
+        return self.project_from(v0, sparse=sparse, pcon=pcon)
+
+    def project_to(self, v0, sparse=True, pcon=False):
+        """State(s) in the full basis -> symmetry-reduced basis, P^dagger v0
+        (base_general.py:584-683).  As in the reference, the sparse form
+        multiplies by the transpose P^T without conjugation."""
+        import scipy.sparse as sp
+        if not self._made_basis:
+            raise AttributeError("this function requires the basis to be cosntructed first, see basis.make().")
+        if not hasattr(v0, "shape"):
+            v0 = np.asanyarray(v0)
+        if v0.ndim not in (1, 2):
+            raise ValueError("excpecting v0 to have ndim > 0 and at most 2")
+        Ns_full = self._proj_device(pcon)[3]
+        if v0.shape[0] != Ns_full:
+            raise ValueError("v0 shape {0} not compatible with Ns_full={1}".format(v0.shape, Ns_full))
+        if sp.issparse(v0):
+            raise ValueError
+        if sparse:
+            vh = D.to_host(v0) if D.is_device_array(v0) else np.ascontiguousarray(v0)
+            if vh.ndim == 1:
+                vh = vh.reshape(-1, 1)
+            return self.get_proj(vh.dtype, pcon=pcon).T.dot(sp.csr_matrix(vh))
+        return self._project(v0, 1, pcon)
+
     def __repr__(self):
         return "<{} N={} Ns={} blocks={}>".format(type(self).__name__, self._N, self._Ns, self._blocks)
 

@@ -1450,3 +1450,251 @@ extern "C" int qs_csr_t_fill(int vtype, int64_t n, const void *indptr, int idx64
     if (n >= ((int64_t)1 << (64 - TERM_BITS - POS_BITS))) return QS_ERR_UNSUPPORTED;
     DISPATCH_VT(vtype, csr_t_fill_t, n, indptr, idx64, indices, data, rowptr, cursor, keys, vals, qs_stream(stream));
 }
+
+// ---------------------------------------------------------------------------
+// projector from the symmetry-reduced basis to the full (or the
+// particle-conserving) basis: the reference's basis.get_proj / project_from /
+// project_to (src/quspin/basis/basis_general/base_general.py:521-718).
+//
+// Column i is the symmetric state of representative s_i,
+//     |psi_i> = c_i sum_{g in G} chi(g) sigma(g, s_i) |g s_i>,
+//     c_i = 1 / sqrt(n_i prod_k per_k),
+// summed over the odometer's group elements (maps applied map 0 first), with
+// chi(g) the phase-table entry and sigma the fermion sign of g -- the pair
+// term_element applies to a matrix element, so that P^dagger H_full P
+// reproduces the sector matrix.  Elements reaching the same image are summed
+// (for commuting maps the n_i elements of a coset carry the same chi sigma,
+// so an image gets sqrt(n_i / |G|) chi sigma; for maps that do not commute
+// the sums can differ or cancel).  Images whose summed unit phases fall
+// below 1e-12 are dropped.  One warp per column: every group element is
+// formed, the images are sorted descending in shared memory (bitonic), runs
+// are summed and the entries written in ascending row order.  Two passes:
+// mode 0 counts the entries of each column, mode 1 writes them.
+
+#define PROJ_DROP 1e-12
+
+template <typename S>
+__global__ void proj_kernel(SymView<S> V, size_t tab_elems, const S *__restrict__ states,
+                            const uint32_t *__restrict__ norms, int64_t Ns, int gsize, int gpow2, int pcon,
+                            BasisView Pc, int mode, int64_t *__restrict__ colptr, int64_t *__restrict__ rows,
+                            double *__restrict__ vals, int *__restrict__ d_err)
+{
+    extern __shared__ unsigned char smem_raw[];
+    stage_tables(V, reinterpret_cast<S *>(smem_raw), tab_elems);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const size_t tab_bytes = (tab_elems * sizeof(S) + 15) & ~(size_t)15;
+    S *key = reinterpret_cast<S *>(smem_raw + tab_bytes) + (size_t)warp * gpow2;
+    int *aux = reinterpret_cast<int *>(smem_raw + tab_bytes + (size_t)wpb * gpow2 * sizeof(S)) + (size_t)warp * gpow2;
+    const int K = V.nmaps;
+    const S full_mask = (V.N >= (int)(8 * sizeof(S))) ? ~(S)0 : (((S)1 << V.N) - 1);
+    int err = 0;
+    for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < Ns; i += (int64_t)gridDim.x * wpb) {
+        const S s = states[i];
+        for (int e = lane; e < gpow2; e += 32) {
+            S t = s;
+            int sg = 1, ph = 0, pad = 0;
+            if (e < gsize) {
+                int rem = e;
+                int dig[QS_MAXMAPS];
+                for (int d = K - 1; d >= 0; d--) { dig[d] = rem % V.pers[d]; rem /= V.pers[d]; }
+                for (int d = 0; d < K; d++) {
+                    for (int r = 0; r < dig[d]; r++) t = map_state(V, d, t, sg);
+                    ph = (int)((ph + (int64_t)dig[d] * V.step[d]) % V.L);
+                }
+            } else {
+                pad = 1;   // padding: a copy of s that adds nothing to the sums
+            }
+            key[e] = t;
+            aux[e] = ph | (sg < 0 ? (1 << 30) : 0) | (pad << 29);
+        }
+        __syncwarp();
+        for (int k = 2; k <= gpow2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int e = lane; e < gpow2; e += 32) {
+                    const int x = e ^ j;
+                    if (x > e) {
+                        const S a = key[e], b = key[x];
+                        const bool desc = (e & k) == 0;
+                        if (desc ? (a < b) : (a > b)) {
+                            key[e] = b; key[x] = a;
+                            const int t = aux[e]; aux[e] = aux[x]; aux[x] = t;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        const int64_t c0 = mode ? colptr[i] : 0, cnt = mode ? colptr[i + 1] - c0 : 0;
+        const double c = 1.0 / sqrt((double)norms[i] * (double)gsize);
+        int64_t base = 0;
+        for (int e0 = 0; e0 < gpow2; e0 += 32) {
+            const int e = e0 + lane;
+            bool keep = false;
+            double re = 0.0, im = 0.0;
+            if (e < gpow2 && (e == 0 || key[e] != key[e - 1])) {
+                const S t = key[e];
+                for (int f = e; f < gpow2 && key[f] == t; f++) {
+                    const int a = aux[f];
+                    if ((a >> 29) & 1) continue;
+                    const int ph = a & ((1 << 29) - 1);
+                    const double sgn = ((a >> 30) & 1) ? -1.0 : 1.0;
+                    re += sgn * V.ph_re[ph];
+                    im += sgn * V.ph_im[ph];
+                }
+                keep = hypot(re, im) > PROJ_DROP;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (keep && mode) {
+                const int64_t pos = base + __popc(bal & ((1u << lane) - 1u));
+                if (pos < cnt) {
+                    const S t = key[e];
+                    int64_t row;
+                    if (pcon) row = find_index<S>(Pc, V.N, t);
+                    else row = (int64_t)(full_mask - t);
+                    if (row < 0) err |= 4;
+                    rows[c0 + pos] = row;
+                    vals[2 * (c0 + pos)] = c * re;
+                    vals[2 * (c0 + pos) + 1] = c * im;
+                } else {
+                    err |= 2;
+                }
+            }
+            base += __popc(bal);
+        }
+        if (lane == 0) {
+            if (!mode) colptr[i + 1] = base;
+            else if (base != cnt) err |= 2;
+        }
+        __syncwarp();
+    }
+    if (err) atomicOr(d_err, err);
+}
+
+static int proj_layout(const QsSym *q, int gsize, int &gpow2, int &wpb, size_t &smem)
+{
+    if (gsize < 1 || gsize > 8192) return QS_ERR_UNSUPPORTED;
+    gpow2 = 1;
+    while (gpow2 < gsize) gpow2 <<= 1;
+    wpb = 4;
+    while (wpb > 1 && (size_t)wpb * gpow2 * (q->sbytes + 4) > 96 * 1024) wpb >>= 1;
+    smem = ((q->tab_bytes + 15) & ~(size_t)15) + (size_t)wpb * gpow2 * (q->sbytes + 4);
+    return smem > 200 * 1024 ? QS_ERR_UNSUPPORTED : QS_OK;
+}
+
+// Entries of the projector, column by column (CSC).  gsize = |G| (product
+// of the map periods, <= 8192).  mode 0: colptr[i + 1] = number of entries
+// of column i (colptr int64[Ns + 1]; the caller sets colptr[0] = 0 and turns
+// the counts into offsets); mode 1: rows int64[colptr[Ns]] and vals
+// complex128[colptr[Ns]] written from those offsets.
+// pcon = 0: rows index the full space, row = 2^N - 1 - state (N <= 62);
+// pcon = 1: rows index the particle-conserving basis given by p_states ...
+// p_end (descending states with prefix blocks, as qs_index takes them).
+// d_err bits: 2 count mismatch between the passes, 4 image outside the row
+// basis.
+extern "C" int qs_proj_fill(void *sym, const void *states, const uint32_t *norms, int64_t Ns, int gsize, int mode,
+                            int64_t *colptr, int pcon, const void *p_states, int64_t p_Ns, int p_N_p,
+                            const int64_t *p_begin, const int64_t *p_end, int64_t *rows, void *vals, int *d_err,
+                            void *stream)
+{
+    const QsSym *q = reinterpret_cast<const QsSym *>(sym);
+    if (!q || Ns < 0 || !d_err || (mode != 0 && mode != 1)) return QS_ERR_ARG;
+    if (Ns > 0 && (!states || !norms || !colptr || (mode == 1 && (!rows || !vals)))) return QS_ERR_ARG;
+    if (pcon && mode == 1 && (!p_states || p_Ns < 0)) return QS_ERR_ARG;
+    if (!pcon && q->N > 62) return QS_ERR_UNSUPPORTED;
+    int prod = 1;
+    for (int d = 0; d < q->nmaps; d++) {
+        prod *= q->pers[d];
+        if (prod > 8192) return QS_ERR_UNSUPPORTED;
+    }
+    if (prod != gsize) return QS_ERR_ARG;
+    if (Ns == 0) return QS_OK;
+    int gpow2, wpb;
+    size_t sm;
+    int rc = proj_layout(q, gsize, gpow2, wpb, sm);
+    if (rc) return rc;
+    BasisView Pc{p_states, nullptr, p_Ns, p_N_p, p_begin, p_end};
+    cudaStream_t st = qs_stream(stream);
+    int64_t b = (Ns + wpb - 1) / wpb, cap = (int64_t)qs_num_sms() * 16;
+    const unsigned blocks = (unsigned)(b > cap ? cap : b);
+    if (q->sbytes == 4) {
+        auto k = proj_kernel<uint32_t>;
+        if ((rc = set_smem(k, sm))) return rc;
+        k<<<blocks, 32 * wpb, sm, st>>>(make_view<uint32_t>(q), q->tab_bytes / 4, (const uint32_t *)states, norms,
+                                        Ns, gsize, gpow2, pcon, Pc, mode, colptr, rows, (double *)vals, d_err);
+    } else {
+        auto k = proj_kernel<uint64_t>;
+        if ((rc = set_smem(k, sm))) return rc;
+        k<<<blocks, 32 * wpb, sm, st>>>(make_view<uint64_t>(q), q->tab_bytes / 8, (const uint64_t *)states, norms,
+                                        Ns, gsize, gpow2, pcon, Pc, mode, colptr, rows, (double *)vals, d_err);
+    }
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+namespace {
+
+// y[rows[e], c] += P[e] x[i, c] for the entries e of column i (one warp per
+// column; the columns of one projector own disjoint rows -- disjoint
+// orbits -- so no atomics).
+__global__ void proj_from_kernel(int64_t Ns, const int64_t *__restrict__ colptr, const int64_t *__restrict__ rows,
+                                 const cdbl *__restrict__ P, const cdbl *__restrict__ x, int64_t k,
+                                 cdbl *__restrict__ y)
+{
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (int64_t i = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); i < Ns; i += (int64_t)gridDim.x * wpb)
+        for (int64_t e = colptr[i] + lane; e < colptr[i + 1]; e += 32) {
+            const cdbl p = P[e];
+            const int64_t r = rows[e];
+            for (int64_t c = 0; c < k; c++) {
+                const cdbl v = x[i * k + c];
+                cdbl *o = y + r * k + c;
+                o->x += p.x * v.x - p.y * v.y;
+                o->y += p.x * v.y + p.y * v.x;
+            }
+        }
+}
+
+// y[i, c] = sum_e conj(P[e]) x[rows[e], c] (one warp per column, fixed-order
+// lane partials and butterfly sum).
+__global__ void proj_to_kernel(int64_t Ns, const int64_t *__restrict__ colptr, const int64_t *__restrict__ rows,
+                               const cdbl *__restrict__ P, const cdbl *__restrict__ x, int64_t k,
+                               cdbl *__restrict__ y)
+{
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (int64_t i = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); i < Ns; i += (int64_t)gridDim.x * wpb)
+        for (int64_t c = 0; c < k; c++) {
+            double re = 0.0, im = 0.0;
+            for (int64_t e = colptr[i] + lane; e < colptr[i + 1]; e += 32) {
+                const cdbl p = P[e];
+                const cdbl v = x[rows[e] * k + c];
+                re += p.x * v.x + p.y * v.y;
+                im += p.x * v.y - p.y * v.x;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) y[i * k + c] = cdbl{re, im};
+        }
+}
+
+}  // namespace
+
+// direction 0 (project_from): y[Nfull, k] += P x (zero y first for P x;
+// several symmetry sectors accumulate into one full-space state);
+// direction 1 (project_to): y[Ns, k] = P^dagger x.  Complex128, C order.
+extern "C" int qs_proj_apply(int direction, int64_t Ns, const int64_t *colptr, const int64_t *rows, const void *P,
+                             const void *x, int64_t k, void *y, void *stream)
+{
+    if (Ns < 0 || k < 1 || (direction != 0 && direction != 1)) return QS_ERR_ARG;
+    if (Ns == 0) return QS_OK;
+    if (!colptr || !rows || !P || !x || !y) return QS_ERR_ARG;
+    cudaStream_t st = qs_stream(stream);
+    int64_t b = (Ns + 7) / 8, cap = (int64_t)qs_num_sms() * 16;
+    const unsigned blocks = (unsigned)(b > cap ? cap : b);
+    if (direction == 0)
+        proj_from_kernel<<<blocks, 256, 0, st>>>(Ns, colptr, rows, (const cdbl *)P, (const cdbl *)x, k, (cdbl *)y);
+    else
+        proj_to_kernel<<<blocks, 256, 0, st>>>(Ns, colptr, rows, (const cdbl *)P, (const cdbl *)x, k, (cdbl *)y);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}

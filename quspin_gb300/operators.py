@@ -301,13 +301,14 @@ class hamiltonian:
                 self._union = DeviceCSR.from_scipy(self._static.tocsr(), self._dtype)
             return self._union
         if self._union is None:
-            parts = [self._static.tocsr()] + [Hd.tocsr() for Hd in self._dynamic.values()]
-            pat = parts[0].copy().astype(np.float64)
-            pat.data[:] = 1.0
+            parts = [sp.csr_matrix(p) for p in
+                     [self._static.tocsr()] + [Hd.tocsr() for Hd in self._dynamic.values()]]
+
+            def ones(p):
+                return sp.csr_matrix((np.ones(p.nnz), p.indices, p.indptr), shape=p.shape)
+            pat = ones(parts[0])
             for p in parts[1:]:
-                q = p.copy().astype(np.float64)
-                q.data[:] = 1.0
-                pat = pat + q
+                pat = pat + ones(p)
             pat = sp.csr_matrix(pat)
             pat.sort_indices()
             vals = []

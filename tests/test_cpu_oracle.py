@@ -155,3 +155,38 @@ def test_oracle_ftlm_ltlm_match_reference_golden():
     np.testing.assert_allclose(Ol["H"], g["ltlm_H"], rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(Ol["Czz"], g["ltlm_C"], rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(Il, g["ltlm_I"], rtol=1e-12)
+
+
+def _proj_cases():
+    """(N, sectors, fermion, blocks, static) of small sectors, complex momenta
+    and fermion signs included."""
+    m = chain_maps(8)
+    xxz = xxz_static(8)
+    hop = [["+-", [[-1.0, i, (i + 1) % 8] for i in range(8)]], ["-+", [[1.0, i, (i + 1) % 8] for i in range(8)]],
+           ["nn", [[0.7, i, (i + 1) % 8] for i in range(8)]]]
+    cases = []
+    for k in (0, 1, 2, 3, 4):
+        cases.append((8, [(1, 4, 0)], False, dict(kblock=(m["t"], k)), xxz))
+    cases.append((8, [(1, 4, 0)], False, dict(kblock=(m["t"], 0), pblock=(m["p"], 1), zblock=(m["z"], 0)), xxz))
+    cases.append((8, [(0, 0, 0)], False, dict(zblock=(m["z"], 1), kblock=(m["t"], 3)), xxz))
+    for Nf, k in ((3, 1), (4, 0), (4, 2), (3, 5)):
+        cases.append((8, [(1, Nf, 0)], True, dict(kblock=(m["t"], k)), hop))
+    return cases
+
+
+def test_oracle_projector_invariants():
+    """P^dagger P = 1 and P^dagger H_full P = H_sector (the reference checks
+    projected Hamiltonians this way: test/test_project_op.py,
+    test/test_ham_project_to.py), with rows in the full space and in the
+    particle-conserving basis."""
+    for N, sectors, fermion, blocks, static in _proj_cases():
+        ob = O.OracleBasis(N, sectors, fermion=fermion, pauli=0, **blocks)
+        H = O.make_static(ob, static, np.complex128)
+        full = O.OracleBasis(N, [(0, 0, 0)], fermion=fermion, pauli=0)
+        pcon = O.OracleBasis(N, sectors, fermion=fermion, pauli=0)
+        for rowb, P in ((full, ob.get_proj(np.complex128)), (pcon, ob.get_proj(np.complex128, pcon_basis=pcon))):
+            assert P.shape == (rowb.Ns, ob.Ns)
+            Ph = P.conj().T
+            np.testing.assert_allclose((Ph @ P).toarray(), np.eye(ob.Ns), atol=1e-14)
+            Hf = O.make_static(rowb, static, np.complex128)
+            np.testing.assert_allclose((Ph @ Hf @ P).toarray(), H.toarray(), atol=1e-13)
