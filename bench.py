@@ -265,6 +265,122 @@ def time_kernels(op, F, reps=20):
     return t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8
 
 
+def library_spmv(A, F, n_bytes, reps=20):
+    """Context for the roofline, not a product path: the vendor sparse library
+    (cuSPARSE through ctypes) on the same CSR arrays, for the product ours
+    computes (real matrix times the complex state), in the two ways a cuSPARSE
+    user would write it: one SpMM on the state viewed as a row-major [n, 2]
+    float64 block, or two real SpMVs on the de-interleaved real and imaginary
+    parts.  Each is the fastest of the CSR algorithms that accept the operands;
+    GB/s counts our algorithmic bytes n_bytes.  Returns a dict."""
+    import ctypes
+    import torch
+    lib = None
+    for name in ("libcusparse.so.12", "libcusparse.so", "/usr/local/cuda/lib64/libcusparse.so.12"):
+        try:
+            lib = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    if lib is None:
+        return {"unavailable": "libcusparse not found"}
+    if A.idx64:
+        return {"unavailable": "int64 row offsets"}
+    vp, i64 = ctypes.c_void_p, ctypes.c_int64
+    R64F, IDX32, BASE0, ROW, NOTRANS = 1, 2, 0, 2, 0
+    n = A.shape[0]
+    one, zero = ctypes.c_double(1.0), ctypes.c_double(0.0)
+    st = torch.cuda.current_stream()
+    handles = []
+
+    def ok(rc, what):
+        if rc != 0:
+            raise RuntimeError("{} returned {}".format(what, rc))
+
+    def timed(run):
+        for _ in range(3):
+            if run() != 0:
+                return None
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            run()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    out = {}
+    h, matA = vp(), vp()
+    try:
+        ok(lib.cusparseCreate(ctypes.byref(h)), "cusparseCreate")
+        ok(lib.cusparseSetStream(h, vp(st.cuda_stream)), "cusparseSetStream")
+        ok(lib.cusparseCreateCsr(ctypes.byref(matA), i64(n), i64(n), i64(A.nnz), vp(A.indptr.data_ptr()),
+                                 vp(A.indices.data_ptr()), vp(A.data.data_ptr()), IDX32, IDX32, BASE0, R64F),
+           "cusparseCreateCsr")
+        ref = torch.view_as_real(A.matvec_into(F, torch.empty_like(F)).reshape(-1))
+        # one SpMM on [n, 2]
+        X = torch.view_as_real(F.reshape(-1)).contiguous()
+        Y = torch.empty_like(X)
+        matB, matC = vp(), vp()
+        ok(lib.cusparseCreateDnMat(ctypes.byref(matB), i64(n), i64(2), i64(2), vp(X.data_ptr()), R64F, ROW), "DnMat")
+        handles.append(("cusparseDestroyDnMat", matB))
+        ok(lib.cusparseCreateDnMat(ctypes.byref(matC), i64(n), i64(2), i64(2), vp(Y.data_ptr()), R64F, ROW), "DnMat")
+        handles.append(("cusparseDestroyDnMat", matC))
+        best = None
+        for alg, name in ((0, "ALG_DEFAULT"), (6, "CSR_ALG2"), (12, "CSR_ALG3")):
+            size = ctypes.c_size_t(0)
+            if lib.cusparseSpMM_bufferSize(h, NOTRANS, NOTRANS, ctypes.byref(one), matA, matB, ctypes.byref(zero),
+                                           matC, R64F, alg, ctypes.byref(size)) != 0:
+                continue
+            buf = torch.empty(max(int(size.value), 16), dtype=torch.uint8, device=F.device)
+            t = timed(lambda: lib.cusparseSpMM(h, NOTRANS, NOTRANS, ctypes.byref(one), matA, matB,
+                                               ctypes.byref(zero), matC, R64F, alg, vp(buf.data_ptr())))
+            if t is not None and (best is None or t < best[0]):
+                best = (t, name, float((Y - ref).abs().max() / ref.abs().max()))
+        if best:
+            out["spmm_n2"] = {"impl": "cuSPARSE SpMM {} (float64 CSR x row-major [n, 2])".format(best[1]),
+                              "ms": 1e3 * best[0], "gbs": n_bytes / best[0] / 1e9, "max_rel_diff": best[2]}
+        # two real SpMVs
+        xr, xi = X[:, 0].contiguous(), X[:, 1].contiguous()
+        yr, yi = torch.empty_like(xr), torch.empty_like(xi)
+        vx = [vp() for _ in range(4)]
+        for d, t_ in zip(vx, (xr, xi, yr, yi)):
+            ok(lib.cusparseCreateDnVec(ctypes.byref(d), i64(n), vp(t_.data_ptr()), R64F), "DnVec")
+            handles.append(("cusparseDestroyDnVec", d))
+        best = None
+        for alg, name in ((0, "ALG_DEFAULT"), (2, "CSR_ALG1"), (3, "CSR_ALG2")):
+            size = ctypes.c_size_t(0)
+            if lib.cusparseSpMV_bufferSize(h, NOTRANS, ctypes.byref(one), matA, vx[0], ctypes.byref(zero), vx[2],
+                                           R64F, alg, ctypes.byref(size)) != 0:
+                continue
+            buf = torch.empty(max(int(size.value), 16), dtype=torch.uint8, device=F.device)
+
+            def two():
+                r0 = lib.cusparseSpMV(h, NOTRANS, ctypes.byref(one), matA, vx[0], ctypes.byref(zero), vx[2], R64F,
+                                      alg, vp(buf.data_ptr()))
+                return r0 or lib.cusparseSpMV(h, NOTRANS, ctypes.byref(one), matA, vx[1], ctypes.byref(zero), vx[3],
+                                              R64F, alg, vp(buf.data_ptr()))
+            t = timed(two)
+            if t is not None and (best is None or t < best[0]):
+                diff = float(torch.maximum((yr - ref[:, 0]).abs().max(), (yi - ref[:, 1]).abs().max())
+                             / ref.abs().max())
+                best = (t, name, diff)
+        if best:
+            out["spmv_x2"] = {"impl": "cuSPARSE SpMV {} twice (float64 CSR x real and imaginary parts)".format(best[1]),
+                              "ms": 1e3 * best[0], "gbs": n_bytes / best[0] / 1e9, "max_rel_diff": best[2]}
+    except Exception as exc:           # the comparison is optional
+        out["unavailable"] = str(exc).splitlines()[0][:120]
+    finally:
+        for fn, d in reversed(handles):
+            getattr(lib, fn)(d)
+        if matA.value:
+            lib.cusparseDestroySpMat(matA)
+        if h.value:
+            lib.cusparseDestroy(h)
+    return out
+
+
 def cpu_baseline(H, op, terms_per_evolution, budget_s=12.0):
     """Oracle OpenMP Taylor loop on the host cores over a bounded sample of
     Taylor terms of this evolution; evolutions/s scaled by the executed term
@@ -373,6 +489,7 @@ def run_ours(args, rank, ws):
     rel_err = float(torch.linalg.vector_norm(F_pair - F) / torch.linalg.vector_norm(F))
     op.precision = "double"
     t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8 = time_kernels(op, v_dev)
+    lib_ctx = library_spmv(A, v_dev, spmv_bytes(n, nnz)) if A.dtype == np.float64 else {"unavailable": "complex"}
     peak, peak_kind = peak_hbm()
     tb = taylor_term_bytes(n, nnz)
     achieved = tb / t_term / 1e9
@@ -398,7 +515,8 @@ def run_ours(args, rank, ws):
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
                      "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff},
                      "spmv_gbs": spmv_bytes(n, nnz) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
-                     "spmm8_gbs": spmv_bytes(n, nnz, 8) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8},
+                     "spmm8_gbs": spmv_bytes(n, nnz, 8) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
+                     "library_spmv": lib_ctx},
         "gpu_launches": int(args.steps * launches_per_evolution),
         "clocks": clk.summary(),
         "state_norm_error": norm_err,
