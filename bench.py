@@ -171,15 +171,16 @@ def build_problem(L, J1, J2):
     return b, H
 
 
-def taylor_term_bytes(n, nnz, nvec=1):
-    """Algorithmic bytes of one fused Taylor term, float64 values, int32
-    indices, complex128 B and F: values+indices once, indptr once, B gathered
+def taylor_term_bytes(n, nnz, nvec=1, vb=8):
+    """Algorithmic bytes of one fused Taylor term, int32 indices, complex128
+    B and F: values (vb bytes per nonzero: 8 for one float pair, 1 for a code
+    byte into the 256-entry table) and indices once, indptr once, B gathered
     once (compulsory), new B written, F read and written."""
-    return nnz * (8 + 4) + 4 * (n + 1) + n * nvec * (16 + 16 + 2 * 16)
+    return nnz * (vb + 4) + 4 * (n + 1) + n * nvec * (16 + 16 + 2 * 16)
 
 
-def spmv_bytes(n, nnz, nvec=1):
-    return nnz * (8 + 4) + 4 * (n + 1) + n * nvec * (16 + 16)
+def spmv_bytes(n, nnz, nvec=1, vb=8):
+    return nnz * (vb + 4) + 4 * (n + 1) + n * nvec * (16 + 16)
 
 
 def evolution_term_times(op, F):
@@ -491,7 +492,9 @@ def run_ours(args, rank, ws):
     t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8 = time_kernels(op, v_dev)
     lib_ctx = library_spmv(A, v_dev, spmv_bytes(n, nnz)) if A.dtype == np.float64 else {"unavailable": "complex"}
     peak, peak_kind = peak_hbm()
-    tb = taylor_term_bytes(n, nnz)
+    P = A.paired()
+    vb = P.value_bytes
+    tb = taylor_term_bytes(n, nnz, vb=vb)
     achieved = tb / t_term / 1e9
     # rescale (norm + load) + s (m* terms + norm + load); copy excluded
     launches_per_evolution = 2 + op.s * (op.m_star + 2)
@@ -513,9 +516,12 @@ def run_ours(args, rank, ws):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_lp_kernel",
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
-                     "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff},
-                     "spmv_gbs": spmv_bytes(n, nnz) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
-                     "spmm8_gbs": spmv_bytes(n, nnz, 8) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
+                     "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff,
+                                      "blocks_per_sm_cap": {0: None, 1: 6, 2: 8}[(group >> 18) & 3]},
+                     "value_bytes_per_nonzero": vb, "distinct_values": getattr(P, "distinct", None),
+                     "gathers_per_s": nnz / t_term,
+                     "spmv_gbs": spmv_bytes(n, nnz, vb=vb) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
+                     "spmm8_gbs": spmv_bytes(n, nnz, 8, vb=vb) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
                      "library_spmv": lib_ctx},
         "gpu_launches": int(args.steps * launches_per_evolution),
         "clocks": clk.summary(),

@@ -10,7 +10,9 @@
  *   -6 unsupported configuration, -7 iteration cap reached.
  * Element type codes: 0 float32, 1 float64, 2 complex64, 3 complex128,
  * 4 real value as a float pair hi + lo (8 bytes), 5 complex value as two
- * float pairs {re.hi, re.lo, im.hi, im.lo} (16 bytes).
+ * float pairs {re.hi, re.lo, im.hi, im.lo} (16 bytes); as matrix values
+ * only: 6 / 7 the values of 4 / 5 coded -- a table of 256 such values
+ * followed by one uint8 code per nonzero (int32 column indices only).
  *
  * Each declaration names the reference interface it replaces (QuSpin 1.0.1;
  * paths relative to the reference project root; "html" = the Sphinx

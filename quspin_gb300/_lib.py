@@ -18,7 +18,7 @@ _lib = None
 _lock = threading.Lock()
 
 # element type codes shared with the C side
-F32, F64, C64, C128, PF, CPF = 0, 1, 2, 3, 4, 5
+F32, F64, C64, C128, PF, CPF, PF8, CPF8 = 0, 1, 2, 3, 4, 5, 6, 7
 
 STATUS = {
     -1: "invalid argument",

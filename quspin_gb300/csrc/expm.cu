@@ -332,6 +332,7 @@ extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, i
         const int co = group > 0 && ((group >> 16) & 1) && rownorm != nullptr;
         LpTerm a{n, indptr, idx64, indices, data, dtype, Bin, Bout, btype, Fp, nvec, mu, nullptr, nullptr, cf, j, tol,
                  ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
+        a.occ = group > 0 ? (group >> 18) & 3 : 0;
         return lp_taylor_term(a, false);
     }
     if (btype == QS_C128) {
@@ -656,6 +657,7 @@ extern "C" int qs_taylor_multi_term_rows(int64_t n, const void *indptr, const in
         const int co = group > 0 && ((group >> 16) & 1) && rownorm != nullptr;
         LpTerm a{n, indptr, 0, indices, data, dtype, Bin, Bout, btype, Fp, nvec, cdbl{0.0, 0.0}, m, sec_off, cf, j, tol,
                  ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
+        a.occ = group > 0 ? (group >> 18) & 3 : 0;
         return lp_taylor_term(a, true);
     }
     if (btype == QS_C128) {

@@ -121,6 +121,7 @@ struct LpTerm {
     int narrow;               // chunk-outer with 4-vector chunks instead of 8
     void *rownorm;            // n float pairs of row-sum scratch for chunk_outer, or null
     cudaStream_t st;
+    int occ = 0;              // single-vector float-pair shapes: 1 / 2 cap registers for 6 / 8 blocks per SM
 };
 
 int lp_taylor_term(const LpTerm &a, bool multi);

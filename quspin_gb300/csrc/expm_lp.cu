@@ -8,7 +8,12 @@
 //   * QS_CPF  - paired single precision (csrc/pairf.cuh): B and the matrix
 //               values are hi + lo float pairs, products and row sums run in
 //               FP32 instructions with 48-bit significands; the default
-//               "double" form of the Python layer;
+//               "double" form of the Python layer.  The values come either
+//               as one pair per nonzero (QS_PF / QS_CPF) or, for matrices
+//               with at most 256 distinct values, as one code byte per
+//               nonzero into a table of pairs (QS_PF8 / QS_CPF8): 1 byte of
+//               value stream per nonzero instead of 8 or 16, same pairs,
+//               same arithmetic, bit-identical results;
 //   * QS_C64  - complex64 B and float32 / complex64 values with FP32 row sums:
 //               the mixed form.
 //
@@ -25,6 +30,7 @@
 // two per nonzero.  Row norms for the stopping test are taken in FP32 from
 // the scaled values.
 #include "qs_common.cuh"
+#include <type_traits>
 #include "expm_ctl.cuh"
 #include "pairf.cuh"
 #include "lp_modes.cuh"
@@ -32,8 +38,10 @@
 namespace {
 
 // One Taylor term; MULTI: block-diagonal stack of sectors (MultiCtl), else one
-// matrix (ExpmCtl).  lgG: log2 of the lanes per row.
-template <class M, class DV, class IT, int NB, int U, bool MULTI>
+// matrix (ExpmCtl).  lgG: log2 of the lanes per row.  CODED: data holds a
+// table of QS_CODE_TABLE values followed by one code byte per nonzero
+// (dtype QS_PF8 / QS_CPF8); the table is staged in shared memory.
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
 __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__restrict__ indptr,
                                                         const int32_t *__restrict__ indices,
                                                         const DV *__restrict__ data,
@@ -85,6 +93,12 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
     }
     if (threadIdx.x == 32) s_cf[0] = M::from_d(coeff[j].x);
     if (threadIdx.x == 33) s_cf[1] = M::from_d(coeff[j].y);
+    __shared__ DV s_tab[CODED ? QS_CODE_TABLE : 1];
+    const uint8_t *codes = nullptr;
+    if constexpr (CODED) {
+        for (int i = threadIdx.x; i < QS_CODE_TABLE; i += blockDim.x) s_tab[i] = ldv(data + i);
+        codes = reinterpret_cast<const uint8_t *>(data + QS_CODE_TABLE);
+    }
     __syncthreads();
 
     const int G = 1 << lgG;
@@ -143,7 +157,8 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                     const IT kk = k + (IT)(u * G);
                     const bool in = kk < k1;
                     col[u] = in ? __ldcs(indices + kk) : 0;
-                    d[u] = in ? ldv(data + kk) : vzero<DV>();
+                    if constexpr (CODED) d[u] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
+                    else d[u] = in ? ldv(data + kk) : vzero<DV>();
                 }
 #pragma unroll
                 for (int u = 0; u < U; u++) {
@@ -274,18 +289,32 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         float2 *__restrict__ rownorm
 #define TAYLOR_LP_ARGS n, lgG, indptr, indices, data, Bin, Bout, F, nvec, mu0, mus, sec_off, coeff, j, tol, ctlp, rownorm
 
-template <class M, class DV, class IT, int NB, int U, bool MULTI>
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
 __global__ void __launch_bounds__(256) taylor_lp_kernel(TAYLOR_LP_PARAMS)
 {
-    taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
+    taylor_lp_body<M, DV, IT, NB, U, MULTI, CODED>(TAYLOR_LP_ARGS);
 }
 
 // The eight-column shapes hold 32 pair accumulators per lane; capping them at
 // three resident blocks per SM keeps 24 warps for the gathers.
-template <class M, class DV, class IT, int NB, int U, bool MULTI>
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
 __global__ void __launch_bounds__(256, 3) taylor_lp_kernel_wide(TAYLOR_LP_PARAMS)
 {
-    taylor_lp_body<M, DV, IT, NB, U, MULTI>(TAYLOR_LP_ARGS);
+    taylor_lp_body<M, DV, IT, NB, U, MULTI, CODED>(TAYLOR_LP_ARGS);
+}
+
+// Single-vector float-pair shapes with the registers capped for 6 or 8
+// resident blocks per SM (more warps to cover the gather latency; the
+// tuner decides whether the cap pays on the matrix at hand).
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
+__global__ void __launch_bounds__(256, 6) taylor_lp_kernel_occ6(TAYLOR_LP_PARAMS)
+{
+    taylor_lp_body<M, DV, IT, NB, U, MULTI, CODED>(TAYLOR_LP_ARGS);
+}
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
+__global__ void __launch_bounds__(256, 8) taylor_lp_kernel_occ8(TAYLOR_LP_PARAMS)
+{
+    taylor_lp_body<M, DV, IT, NB, U, MULTI, CODED>(TAYLOR_LP_ARGS);
 }
 
 // F = eta F (per sector for MULTI) and the row-norm maximum; the last block
@@ -401,47 +430,64 @@ __global__ void split_pairs_kernel(int64_t count, const double *__restrict__ src
     }
 }
 
-template <class M, class DV, class IT, int NB, int U, bool MULTI>
+template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
 int lp_go(const LpTerm &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
     const int blocks = taylor_grid(a.n, a.G);
     float2 *rn = a.chunk_outer ? (float2 *)a.rownorm : nullptr;
+    if constexpr (NB == 1 && U <= 2 && sizeof(IT) == 4 && std::is_same<M, ModePF>::value) {
+        if (a.occ == 1 || a.occ == 2) {
+            auto k = a.occ == 1 ? taylor_lp_kernel_occ6<M, DV, IT, NB, U, MULTI, CODED>
+                                : taylor_lp_kernel_occ8<M, DV, IT, NB, U, MULTI, CODED>;
+            k<<<blocks, 256, 0, a.st>>>(a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data,
+                                        (const typename M::BE *)a.Bin, (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0,
+                                        a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
+            QS_CHECK(cudaGetLastError());
+            return QS_OK;
+        }
+    }
     if constexpr (NB >= 8)
-        taylor_lp_kernel_wide<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+        taylor_lp_kernel_wide<M, DV, IT, NB, U, MULTI, CODED><<<blocks, 256, 0, a.st>>>(
             a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
             (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
     else
-        taylor_lp_kernel<M, DV, IT, NB, U, MULTI><<<blocks, 256, 0, a.st>>>(
+        taylor_lp_kernel<M, DV, IT, NB, U, MULTI, CODED><<<blocks, 256, 0, a.st>>>(
             a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
             (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
 
-template <class M, class DV, class IT, bool MULTI>
+template <class M, class DV, class IT, bool MULTI, bool CODED>
 int lp_nb(const LpTerm &a)
 {
     if (a.nvec == 1) {
         if constexpr (sizeof(IT) == 4) {
-            if (a.U >= 4 && !MULTI) return lp_go<M, DV, IT, 1, 4, MULTI>(a);
-            if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, MULTI>(a);
+            if (a.U >= 4 && !MULTI) return lp_go<M, DV, IT, 1, 4, MULTI, CODED>(a);
+            if (a.U >= 2) return lp_go<M, DV, IT, 1, 2, MULTI, CODED>(a);
         }
-        return lp_go<M, DV, IT, 1, 1, MULTI>(a);
+        return lp_go<M, DV, IT, 1, 1, MULTI, CODED>(a);
     }
-    if (a.nvec == 2) return lp_go<M, DV, IT, 2, 1, MULTI>(a);
-    if (a.nvec <= 4 || (a.chunk_outer && a.narrow)) return lp_go<M, DV, IT, 4, 1, MULTI>(a);
-    return lp_go<M, DV, IT, 8, 1, MULTI>(a);
+    if (a.nvec == 2) return lp_go<M, DV, IT, 2, 1, MULTI, CODED>(a);
+    if (a.nvec <= 4 || (a.chunk_outer && a.narrow)) return lp_go<M, DV, IT, 4, 1, MULTI, CODED>(a);
+    return lp_go<M, DV, IT, 8, 1, MULTI, CODED>(a);
 }
 
-template <class M, class DV, bool MULTI>
+// coded values: int32 column indices only
+template <class M, class DV, bool MULTI, bool CODED = false>
 int lp_idx(const LpTerm &a)
 {
-    if constexpr (!MULTI) {
-        if (a.idx64) return lp_nb<M, DV, int64_t, false>(a);
+    if constexpr (CODED) {
+        if (a.idx64) return QS_ERR_ARG;
+        return lp_nb<M, DV, int32_t, MULTI, true>(a);
+    } else {
+        if constexpr (!MULTI) {
+            if (a.idx64) return lp_nb<M, DV, int64_t, false, false>(a);
+        }
+        return lp_nb<M, DV, int32_t, MULTI, false>(a);
     }
-    return lp_nb<M, DV, int32_t, MULTI>(a);
 }
 
 }  // namespace
@@ -453,6 +499,10 @@ int lp_taylor_term(const LpTerm &a, bool multi)
     if (a.btype == QS_CPF) {
         if (a.dtype == QS_PF) return multi ? lp_idx<ModePF, pf, true>(a) : lp_idx<ModePF, pf, false>(a);
         if (a.dtype == QS_CPF) return multi ? lp_idx<ModePF, cpf, true>(a) : lp_idx<ModePF, cpf, false>(a);
+        if (a.dtype == QS_PF8)
+            return multi ? lp_idx<ModePF, pf, true, true>(a) : lp_idx<ModePF, pf, false, true>(a);
+        if (a.dtype == QS_CPF8)
+            return multi ? lp_idx<ModePF, cpf, true, true>(a) : lp_idx<ModePF, cpf, false, true>(a);
     } else if (a.btype == QS_C64) {
         if (a.dtype == QS_F32) return multi ? lp_idx<ModeF32, float, true>(a) : lp_idx<ModeF32, float, false>(a);
         if (a.dtype == QS_C64)

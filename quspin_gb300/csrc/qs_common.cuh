@@ -19,6 +19,9 @@
 #define QS_C128 3
 #define QS_PF 4        // real value kept as a pair of floats hi + lo (8 bytes)
 #define QS_CPF 5       // complex value kept as two float pairs {re.hi, re.lo, im.hi, im.lo} (16 bytes)
+#define QS_PF8 6       // real float-pair values as codes: QS_CODE_TABLE pairs, then one uint8 code per nonzero
+#define QS_CPF8 7      // complex float-pair values as codes: QS_CODE_TABLE complex pairs, then one uint8 code each
+#define QS_CODE_TABLE 256
 
 #define QS_CHECK(call)                                   \
     do {                                                 \

@@ -68,7 +68,9 @@ template <class M> __device__ __forceinline__ void st_out(cflt *y, int64_t e, in
     *p = r;
 }
 
-template <class M, class DV, bool XC, class YT, class IT, int NB, int U>
+// CODED: data holds a table of QS_CODE_TABLE values followed by one code byte
+// per nonzero (pdtype QS_PF8 / QS_CPF8), the table staged in shared memory.
+template <class M, class DV, bool XC, class YT, class IT, int NB, int U, bool CODED>
 __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const IT *__restrict__ indptr,
                                                       const int32_t *__restrict__ indices,
                                                       const DV *__restrict__ data, const void *__restrict__ xv,
@@ -83,6 +85,12 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
     if (threadIdx.x == 0) s_a[0] = M::from_d(a.x);
     if (threadIdx.x == 1) s_a[1] = M::from_d(a.y);
     if (threadIdx.x == 2) s_k = xnorm ? scale_exp(__longlong_as_double((long long)*xnorm)) : 0;
+    __shared__ DV s_tab[CODED ? QS_CODE_TABLE : 1];
+    const uint8_t *codes = nullptr;
+    if constexpr (CODED) {
+        for (int i = threadIdx.x; i < QS_CODE_TABLE; i += blockDim.x) s_tab[i] = ldv(data + i);
+        codes = reinterpret_cast<const uint8_t *>(data + QS_CODE_TABLE);
+    }
     __syncthreads();
     const cx<S> av{s_a[0], s_a[1]};
     const int k2 = s_k;
@@ -113,7 +121,8 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
                     const IT kk = k + (IT)(u * G);
                     const bool in = kk < k1;
                     col[u] = in ? __ldcs(indices + kk) : 0;
-                    d[u] = in ? ldv(data + kk) : vzero<DV>();
+                    if constexpr (CODED) d[u] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
+                    else d[u] = in ? ldv(data + kk) : vzero<DV>();
                 }
 #pragma unroll
                 for (int u = 0; u < U; u++) {
@@ -201,38 +210,44 @@ static int grid_rows(int64_t n, int G)
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-template <class M, class DV, bool XC, class YT, class IT, int NB, int U>
+template <class M, class DV, bool XC, class YT, class IT, int NB, int U, bool CODED>
 int spmv_go(const SpmvArgs &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
-    spmv_lp_kernel<M, DV, XC, YT, IT, NB, U><<<grid_rows(a.n, a.G), 256, 0, a.st>>>(
+    spmv_lp_kernel<M, DV, XC, YT, IT, NB, U, CODED><<<grid_rows(a.n, a.G), 256, 0, a.st>>>(
         a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, a.x, (YT *)a.y, a.nvec, a.a, a.overwrite,
         a.xnorm);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }
 
-template <class M, class DV, bool XC, class YT, class IT>
+template <class M, class DV, bool XC, class YT, class IT, bool CODED>
 int spmv_nb(const SpmvArgs &a)
 {
     if (a.nvec == 1) {
         if constexpr (sizeof(IT) == 4) {
-            if (a.U >= 4) return spmv_go<M, DV, XC, YT, IT, 1, 4>(a);
-            if (a.U >= 2) return spmv_go<M, DV, XC, YT, IT, 1, 2>(a);
+            if (a.U >= 4) return spmv_go<M, DV, XC, YT, IT, 1, 4, CODED>(a);
+            if (a.U >= 2) return spmv_go<M, DV, XC, YT, IT, 1, 2, CODED>(a);
         }
-        return spmv_go<M, DV, XC, YT, IT, 1, 1>(a);
+        return spmv_go<M, DV, XC, YT, IT, 1, 1, CODED>(a);
     }
-    if (a.nvec == 2) return spmv_go<M, DV, XC, YT, IT, 2, 1>(a);
-    if (a.nvec <= 4) return spmv_go<M, DV, XC, YT, IT, 4, 1>(a);
-    return spmv_go<M, DV, XC, YT, IT, 8, 1>(a);
+    if (a.nvec == 2) return spmv_go<M, DV, XC, YT, IT, 2, 1, CODED>(a);
+    if (a.nvec <= 4) return spmv_go<M, DV, XC, YT, IT, 4, 1, CODED>(a);
+    return spmv_go<M, DV, XC, YT, IT, 8, 1, CODED>(a);
 }
 
-template <class M, class DV, bool XC, class YT>
+// coded values: int32 column indices only
+template <class M, class DV, bool XC, class YT, bool CODED = false>
 int spmv_idx(const SpmvArgs &a)
 {
-    if (a.idx64) return spmv_nb<M, DV, XC, YT, int64_t>(a);
-    return spmv_nb<M, DV, XC, YT, int32_t>(a);
+    if constexpr (CODED) {
+        if (a.idx64) return QS_ERR_ARG;
+        return spmv_nb<M, DV, XC, YT, int32_t, true>(a);
+    } else {
+        if (a.idx64) return spmv_nb<M, DV, XC, YT, int64_t, false>(a);
+        return spmv_nb<M, DV, XC, YT, int32_t, false>(a);
+    }
 }
 
 }  // namespace
@@ -252,7 +267,9 @@ int spmv_lp_single(int64_t n, const void *indptr, int idx64, const int32_t *indi
 
 // y = a A x (overwrite) or y += a A x with float64 / complex128 x and y and
 // the matrix values as float pairs (pdtype QS_PF from float64 values,
-// QS_CPF from complex128 values; a complex matrix needs complex x).
+// QS_CPF from complex128 values; a complex matrix needs complex x), or as
+// one code byte per nonzero into a table of such pairs (QS_PF8 / QS_CPF8:
+// QS_CODE_TABLE pairs, then nnz uint8 codes; int32 indices).
 // xs: scratch of n*nvec*(8 or 16) bytes for the split x; norm: 8 bytes of
 // device scratch.  group as for qs_csr_matvec.
 extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
@@ -264,8 +281,10 @@ extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, i
     if (n == 0) return QS_OK;
     const bool xc = xtype == QS_C128;
     if (!xc && xtype != QS_F64) return QS_ERR_ARG;
-    if (!xc && (a_im != 0.0 || pdtype == QS_CPF)) return QS_ERR_ARG;
-    if (pdtype != QS_PF && pdtype != QS_CPF) return QS_ERR_ARG;
+    const bool cvals = pdtype == QS_CPF || pdtype == QS_CPF8;
+    if (!xc && (a_im != 0.0 || cvals)) return QS_ERR_ARG;
+    if (pdtype != QS_PF && pdtype != QS_CPF && pdtype != QS_PF8 && pdtype != QS_CPF8) return QS_ERR_ARG;
+    if ((pdtype == QS_PF8 || pdtype == QS_CPF8) && idx64) return QS_ERR_ARG;
     int G = group > 0 ? (group & 0xff) : 2;
     int U = group > 0 ? ((group >> 8) & 0xff) : 1;
     if (U < 1) U = 1;
@@ -282,6 +301,8 @@ extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, i
     xsplit_kernel<<<blocks, 256, 0, st>>>(count, (const double *)x, (float2 *)xs, nrm);
     QS_CHECK(cudaGetLastError());
     SpmvArgs s{n, indptr, idx64, indices, pdata, xs, y, nvec, cdbl{a_re, a_im}, overwrite, nrm, G, U, st};
+    if (pdtype == QS_PF8) return xc ? spmv_idx<ModePF, pf, true, cdbl, true>(s) : spmv_idx<ModePF, pf, false, double, true>(s);
+    if (pdtype == QS_CPF8) return spmv_idx<ModePF, cpf, true, cdbl, true>(s);
     if (!xc) return spmv_idx<ModePF, pf, false, double>(s);
     if (pdtype == QS_PF) return spmv_idx<ModePF, pf, true, cdbl>(s);
     return spmv_idx<ModePF, cpf, true, cdbl>(s);

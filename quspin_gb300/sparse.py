@@ -62,12 +62,14 @@ class DeviceCSR:
         """Element type code of the values for the C ABI."""
         return D.code(self.dtype)
 
-    def paired(self):
-        """The values split into float pairs (``PairedCSR``), cached."""
-        p = self.__dict__.get("_paired")
+    def paired(self, coded=True):
+        """The values split into float pairs (``PairedCSR``; coded when the
+        matrix has at most 256 distinct values and ``coded``), cached."""
+        key = "_paired_coded" if coded else "_paired"
+        p = self.__dict__.get(key)
         if p is None:
-            p = PairedCSR(self)
-            self._paired = p
+            p = PairedCSR(self, coded=coded)
+            self.__dict__[key] = p
         return p
 
     @classmethod
@@ -246,21 +248,60 @@ class DeviceDIA:
 
 
 class PairedCSR:
-    """A DeviceCSR whose values are kept as float pairs hi + lo (type codes
-    PF / CPF), the operand form of the paired-single Taylor kernels
-    (csrc/expm_lp.cu).  Shares indptr and indices with its source."""
+    """A DeviceCSR whose values are kept as float pairs hi + lo, the operand
+    form of the paired-single kernels (csrc/expm_lp.cu, csrc/spmv_lp.cu).
+    Shares indptr and indices with its source.
+
+    With ``coded`` (the default) and at most 256 distinct values (int32
+    indices), the values are stored as a table of 256 pairs followed by one
+    code byte per nonzero (type codes PF8 / CPF8): the kernels read 1 byte
+    of value stream per nonzero instead of 8 or 16, with the same pairs and
+    the same arithmetic, so the results are bit-identical.  Otherwise one
+    pair per nonzero (PF / CPF)."""
 
     format = "csr"
+    TABLE = 256
 
-    def __init__(self, M):
+    def __init__(self, M, coded=True):
         self.indptr, self.indices, self.shape, self.idx64 = M.indptr, M.indices, M.shape, M.idx64
         self._nnz = M.nnz
         self.complex = M.dtype.kind == "c"
         self.dtype = np.dtype(np.complex128 if self.complex else np.float64)
         src = M.data.to(D.torch_dtype(self.dtype)).contiguous()
+        self.coded = False
+        if coded and not self.idx64 and src.numel() > 0 and self._encode(src):
+            return
+        self._plain(src)
+
+    def _plain(self, src):
         count = src.numel() * (2 if self.complex else 1)
         self.data = torch.empty(max(2 * count, 2), dtype=torch.float32, device=D.device())
-        _lib.call("qs_split_pairs", count, D.ptr(src), D.ptr(self.data), D.stream())
+        if count:
+            _lib.call("qs_split_pairs", count, D.ptr(src), D.ptr(self.data), D.stream())
+        self.coded = False
+
+    def _encode(self, src):
+        if self.complex:
+            uniq, inv = torch.unique(torch.view_as_real(src), dim=0, return_inverse=True)
+            if uniq.shape[0] > self.TABLE:
+                return False
+            vals = torch.zeros(self.TABLE, 2, dtype=torch.float64, device=D.device())
+            vals[:uniq.shape[0]] = uniq
+        else:
+            uniq, inv = torch.unique(src, return_inverse=True)
+            if uniq.numel() > self.TABLE:
+                return False
+            vals = torch.zeros(self.TABLE, dtype=torch.float64, device=D.device())
+            vals[:uniq.numel()] = uniq
+        count = vals.numel()
+        tbytes = count * 8                       # one float pair (8 bytes) per double
+        buf = torch.empty(tbytes + ((src.numel() + 15) // 16) * 16, dtype=torch.uint8, device=D.device())
+        _lib.call("qs_split_pairs", count, D.ptr(vals), D.ptr(buf), D.stream())
+        buf[tbytes:tbytes + src.numel()].copy_(inv.reshape(-1).to(torch.uint8))
+        self.data = buf
+        self.coded = True
+        self.distinct = int(uniq.shape[0])
+        return True
 
     @property
     def nnz(self):
@@ -268,12 +309,24 @@ class PairedCSR:
 
     @property
     def vcode(self):
+        if self.coded:
+            return _lib.CPF8 if self.complex else _lib.PF8
         return _lib.CPF if self.complex else _lib.PF
 
+    @property
+    def value_bytes(self):
+        """Bytes of value stream per nonzero the kernels read."""
+        return 1 if self.coded else (16 if self.complex else 8)
+
     def refresh(self, data):
-        """Re-split new values (same pattern) into the pair buffer."""
-        count = data.numel() * (2 if self.complex else 1)
-        _lib.call("qs_split_pairs", count, D.ptr(data), D.ptr(self.data), D.stream())
+        """Re-split new values (same pattern) into a one-pair-per-nonzero
+        buffer (a coded operand becomes plain)."""
+        src = data.to(D.torch_dtype(self.dtype)).contiguous()
+        if self.coded:
+            self._plain(src)
+            return
+        count = src.numel() * (2 if self.complex else 1)
+        _lib.call("qs_split_pairs", count, D.ptr(src), D.ptr(self.data), D.stream())
 
 
 def to_device_matrix(A, dtype=None):

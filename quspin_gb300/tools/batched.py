@@ -123,16 +123,17 @@ class MultiSectorExpm:
                   D.ptr(self._soff), D.ptr(self._eta), int(use_eta), D.ptr(self._ctl), D.stream())
 
     def _tune(self):
-        from ..tune import _candidates, _time, encode
+        from ..tune import _candidates, _time, encode, occ_candidates
         if self.n < 65536:
             return 0
         b0 = self._work[: self.n * self.nvec]
         b1 = self._work[self.n * self.nvec:]
         best, best_t = 0, None
-        for G, U in _candidates(self.n, self._A.nnz, self.nvec):
-            if self.nvec == 1 and U > 2:
-                continue
-            code = encode(G, U)
+        codes = [encode(G, U) for G, U in _candidates(self.n, self._A.nnz, self.nvec)
+                 if not (self.nvec == 1 and U > 2)]
+        codes += [encode(G, U) | (occ << 18) for G, U in occ_candidates(self._A, self.nvec, self._btype)
+                  for occ in (1, 2)]
+        for code in codes:
             self._ctl.copy_(self._ctl_tmpl)
             t = _time(lambda: self._term(0, b0, b1, 0.0, code))
             if best_t is None or t < best_t:

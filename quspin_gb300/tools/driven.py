@@ -128,7 +128,7 @@ class DrivenEvolution:
             op, bt = self._op, _lib.C64
         else:
             if self._op is None:
-                self._op = M.paired()
+                self._op = M.paired(coded=False)      # values change every step
             else:
                 self._op.refresh(M.data)
             op, bt = self._op, _lib.CPF

@@ -32,6 +32,15 @@ def _candidates(n, nnz, nvec):
     return [(G, U) for G in Gs for U in Us]
 
 
+def occ_candidates(M, nvec, btype):
+    """Shapes also timed with the registers capped for 6 / 8 resident blocks
+    per SM (bits 18-19 of the launch code): single-vector float-pair terms
+    with int32 indices."""
+    if nvec != 1 or btype != _lib.CPF or getattr(M, "idx64", 0):
+        return []
+    return [(G, U) for G in (2, 4) for U in (1, 2)]
+
+
 def _time(fn, reps=5):
     st = torch.cuda.current_stream()
     for _ in range(2):
@@ -92,6 +101,7 @@ def tune_taylor(M, nvec, btype):
         # (8-vector sweeps never beat the one-sweep order in measurements)
         cands += [(G, U, 3) for G, U, _ in cands]
         rown = torch.empty(2 * n, dtype=torch.float32, device=D.device())
+    cands += [(G, U, occ << 2) for G, U in occ_candidates(M, nvec, btype) for occ in (1, 2)]
     for G, U, ch in cands:
         code = encode(G, U) | (ch << 16)
 

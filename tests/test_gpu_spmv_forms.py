@@ -154,3 +154,49 @@ def test_empty_and_tiny_operators(cuda):
     y0 = torch.empty_like(x0)
     M0.matvec_into(x0, y0)
     assert ExpmMultiplyParallel(A0, a=-1j).dot(np.zeros(0, np.complex128)).shape == (0,)
+
+
+def test_coded_values_bit_identical(cuda):
+    """Matrices with at most 256 distinct values keep one code byte per
+    nonzero into a table of float pairs: products and whole evolutions are
+    bit-identical to the one-pair-per-nonzero operand."""
+    import torch
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    from tests.models import chain_maps, xxz_static
+    from quspin_gb300 import _device as D
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import PairedCSR
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    L = 20
+    m = chain_maps(L)
+    cases = [(spin_basis_general(L, Nup=L // 2, pauli=0, kblock=(m["t"], 0), pblock=(m["p"], 0)), np.float64),
+             (spin_basis_general(L, Nup=L // 2, pauli=0, kblock=(m["t"], 3)), np.complex128)]
+    rng = np.random.default_rng(7)
+    for b, dt in cases:
+        H = hamiltonian(xxz_static(L), [], basis=b, dtype=dt)
+        A = H.tocsr_gpu()
+        P1, P2 = PairedCSR(A, coded=True), PairedCSR(A, coded=False)
+        assert P1.coded and not P2.coded and P1.distinct <= 256
+        n = A.shape[0]
+        x = D.to_device(rng.normal(size=(n, 3)) + 1j * rng.normal(size=(n, 3)))
+        ys = []
+        for P in (P1, P2):
+            y = torch.empty_like(x)
+            xs = torch.empty(2 * x.numel() * 2, dtype=torch.float32, device=x.device)
+            nrm = torch.zeros(1, dtype=torch.int64, device=x.device)
+            for g in (0x202, 0x104):
+                _lib.call("qs_csr_matvec_pairs", n, A.nnz, D.ptr(A.indptr), A.idx64, D.ptr(A.indices), D.ptr(P.data),
+                          P.vcode, D.ptr(x), _lib.C128, D.ptr(y), 3, 0.5, -0.25, 1, g, D.ptr(xs), D.ptr(nrm),
+                          D.stream())
+                ys.append(y.clone())
+        assert torch.equal(ys[0], ys[2]) and torch.equal(ys[1], ys[3])
+        np.testing.assert_allclose(D.to_host(ys[0]), (0.5 - 0.25j) * (A.tocsr() @ D.to_host(x)), rtol=0, atol=1e-12)
+        v = rng.normal(size=n) + 1j * rng.normal(size=n)
+        v /= np.linalg.norm(v)
+        outs = []
+        for coded in (True, False):
+            op = ExpmMultiplyParallel(A, a=-2j)
+            if not coded:
+                op._Ad.__dict__["_paired_coded"] = PairedCSR(op._Ad, coded=False)
+            outs.append(op.dot(D.to_device(v)))
+        assert torch.equal(outs[0], outs[1])
