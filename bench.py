@@ -266,6 +266,39 @@ def time_kernels(op, F, reps=20):
     return t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8
 
 
+def gather_probe(A, F, reps=10):
+    """The gather-rate floor for this matrix (qs_gather_probe: the product's
+    row hand-out and its random 16-byte gathers of the vector, no values, no
+    arithmetic, no epilogue), fastest of G = 2, 4, 8 lanes per row at 6 or 8
+    blocks per SM.  Returns (ms, G, blocks per SM) or None."""
+    import torch
+    from quspin_gb300 import _lib
+    from quspin_gb300 import _device as D
+    if A.idx64:
+        return None
+    y = torch.empty_like(F)
+    st = torch.cuda.current_stream()
+    best = None
+    for G in (2, 4, 8):
+        for bps in (6, 8):
+            def run():
+                _lib.call("qs_gather_probe", A.shape[0], D.ptr(A.indptr), D.ptr(A.indices), D.ptr(F), D.ptr(y), G,
+                          bps, D.stream())
+            for _ in range(2):
+                run()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                run()
+            e1.record(st)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / reps
+            if best is None or t < best[0]:
+                best = (t, G, bps)
+    return best
+
+
 def library_spmv(A, F, n_bytes, reps=20):
     """Context for the roofline, not a product path: the vendor sparse library
     (cuSPARSE through ctypes) on the same CSR arrays, for the product ours
@@ -494,6 +527,7 @@ def run_ours(args, rank, ws):
     peak, peak_kind = peak_hbm()
     P = A.paired()
     vb = P.value_bytes
+    probe = gather_probe(A, v_dev)
     tb = taylor_term_bytes(n, nnz, vb=vb)
     achieved = tb / t_term / 1e9
     # rescale (norm + load) + s (m* terms + norm + load); copy excluded
@@ -520,6 +554,10 @@ def run_ours(args, rank, ws):
                                       "blocks_per_sm_cap": {0: None, 1: 6, 2: 8}[(group >> 18) & 3]},
                      "value_bytes_per_nonzero": vb, "distinct_values": getattr(P, "distinct", None),
                      "gathers_per_s": nnz / t_term,
+                     "gather_probe": None if probe is None else {
+                         "ms": probe[0], "lanes_per_row": probe[1], "blocks_per_sm": probe[2],
+                         "gathers_per_s": nnz / (probe[0] / 1e3),
+                         "kernel_time_over_probe": 1e3 * t_term / probe[0]},
                      "spmv_gbs": spmv_bytes(n, nnz, vb=vb) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
                      "spmm8_gbs": spmv_bytes(n, nnz, 8, vb=vb) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
                      "library_spmv": lib_ctx},

@@ -127,6 +127,13 @@ int qs_proj_fill(void *sym, const void *d_states, const uint32_t *d_norms, int64
 int qs_proj_apply(int direction, int64_t Ns, const int64_t *d_colptr, const int64_t *d_rows, const void *d_P,
                   const void *d_x, int64_t k, void *d_y, void *stream);
 
+/* ---- measurement helper (no reference counterpart) ----------------------
+ * Gather-rate probe for the roofline: y[r] = sum of x[indices[k]] over row r
+ * (16-byte elements), the product kernels' row hand-out without values or
+ * epilogue.  int32 indptr / indices; G in {2, 4, 8}; blocks_per_sm 1..16. */
+int qs_gather_probe(int64_t n, const int32_t *d_indptr, const int32_t *d_indices, const void *d_x, void *d_y, int G,
+                    int blocks_per_sm, void *stream);
+
 /* ---- _matvec for csr / dia (html matvec/matvec_core.html:146-201) ------- */
 int qs_csr_matvec(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                   const void *d_data, int dtype, const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re,

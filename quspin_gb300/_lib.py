@@ -63,6 +63,7 @@ _SIGS = {
     "qs_proj_fill": (_i, [_vp, _vp, _vp, _i64, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp,
                           _vp]),
     "qs_proj_apply": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "qs_gather_probe": (_i, [_i64, _vp, _vp, _vp, _vp, _i, _i, _vp]),
     "qs_csr_matvec": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp]),
     "qs_csr_matvec_pairs": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp, _vp,
                                  _vp]),

@@ -100,6 +100,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         codes = reinterpret_cast<const uint8_t *>(data + QS_CODE_TABLE);
     }
     __syncthreads();
+    const unsigned long long keep = l2_keep_policy();
 
     const int G = 1 << lgG;
     const int GPW = 32 >> lgG;
@@ -166,7 +167,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
 #pragma unroll
                         for (int b = 0; b < NB; b++)
                             if (NB == 1 || c0 + b < nvec)
-                                vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(Bin + (int64_t)col[u] * nvec + c0 + b));
+                                vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(Bin + (int64_t)col[u] * nvec + c0 + b, keep));
                     }
                 }
             }

@@ -10,6 +10,30 @@
 
 namespace {
 
+// L2 eviction priority for the gathered vector (createpolicy, PTX ISA 7.4+):
+// its gathers carry an evict_last policy so that its lines outlive the
+// streamed indices, values and partial sums (loaded and stored evict-first
+// through __ldcs / __stcs) while a product or Taylor term runs.
+__device__ __forceinline__ unsigned long long l2_keep_policy()
+{
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float4 ld_keep4(const float4 *p, unsigned long long pol)
+{
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float2 ld_keep2(const float2 *p, unsigned long long pol)
+{
+    float2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+
 struct ModePF {
     using S = pf;
     using BE = cpf;
@@ -17,6 +41,11 @@ struct ModePF {
     __device__ static BE ldB(const BE *p)
     {
         const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+        return BE{pf{v.x, v.y}, pf{v.z, v.w}};
+    }
+    __device__ static BE ldB(const BE *p, unsigned long long pol)
+    {
+        const float4 v = ld_keep4(reinterpret_cast<const float4 *>(p), pol);
         return BE{pf{v.x, v.y}, pf{v.z, v.w}};
     }
     __device__ static void fma(S &acc, S a, S b) { pf_fma(acc, a.h, a.l, b.h, b.l); }
@@ -56,6 +85,11 @@ struct ModeF32 {
     __device__ static BE ldB(const BE *p)
     {
         const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return BE{v.x, v.y};
+    }
+    __device__ static BE ldB(const BE *p, unsigned long long pol)
+    {
+        const float2 v = ld_keep2(reinterpret_cast<const float2 *>(p), pol);
         return BE{v.x, v.y};
     }
     __device__ static void fma(S &acc, S a, S b) { acc = __fmaf_rn(a, b, acc); }

@@ -1,0 +1,69 @@
+// Gather-rate probe: the roofline reference for the CSR kernels.
+//
+// The single-vector product is bound by the rate at which an SM can serve
+// scattered 16-byte loads, not by HBM bandwidth.  This probe measures that
+// rate on the matrix at hand: per row, the sum of x[col] over the row's
+// column indices (16-byte elements, the float-pair complex layout of B),
+// with the row hand-out of the product kernels (G lanes per row, two
+// entries in flight per lane) and no values, no arithmetic beyond the sums,
+// no epilogue.  Its time is the floor a kernel with this access pattern can
+// reach; bench.py reports the Taylor kernel's time against it.  It is a
+// measurement helper only: no product path calls it.
+#include "qs_common.cuh"
+
+namespace {
+
+__global__ void __launch_bounds__(256) gather_probe_kernel(int64_t n, int lgG, const int32_t *__restrict__ indptr,
+                                                           const int32_t *__restrict__ indices,
+                                                           const float4 *__restrict__ x, float4 *__restrict__ y)
+{
+    const int G = 1 << lgG;
+    const int GPW = 32 >> lgG;
+    const int lane = threadIdx.x & (G - 1);
+    const int gsub = (threadIdx.x & 31) >> lgG;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int64_t r = rb + gsub;
+        const bool valid = r < n;
+        const int32_t k0 = valid ? indptr[r] : 0, k1 = valid ? indptr[r + 1] : 0;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int32_t k = k0 + lane; k < k1; k += 2 * G) {
+            const int32_t c0 = __ldcs(indices + k);
+            const int32_t c1 = k + G < k1 ? __ldcs(indices + k + G) : -1;
+            const float4 v0 = __ldg(x + c0);
+            const float4 v1 = c1 >= 0 ? __ldg(x + c1) : make_float4(0.f, 0.f, 0.f, 0.f);
+            acc.x += v0.x + v1.x;
+            acc.y += v0.y + v1.y;
+            acc.z += v0.z + v1.z;
+            acc.w += v0.w + v1.w;
+        }
+        for (int o = G >> 1; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+            acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+            acc.w += __shfl_xor_sync(0xffffffffu, acc.w, o);
+        }
+        if (valid && lane == 0) y[r] = acc;
+    }
+}
+
+}  // namespace
+
+// y[r] = sum over row r of x[indices[k]] for an n-row CSR with int32 indptr
+// and indices; x, y: 16-byte elements (n of each).  G lanes per row (2, 4, 8);
+// blocks_per_sm: grid size in blocks per SM (1..16).
+extern "C" int qs_gather_probe(int64_t n, const int32_t *indptr, const int32_t *indices, const void *x, void *y,
+                               int G, int blocks_per_sm, void *stream)
+{
+    if (n < 1 || !indptr || !indices || !x || !y) return QS_ERR_ARG;
+    if ((G != 2 && G != 4 && G != 8) || blocks_per_sm < 1 || blocks_per_sm > 16) return QS_ERR_ARG;
+    int lg = 0;
+    while ((1 << lg) < G) lg++;
+    const int64_t rows_pb = 256 / G;
+    const int64_t b = (n + rows_pb - 1) / rows_pb, cap = (int64_t)qs_num_sms() * blocks_per_sm;
+    gather_probe_kernel<<<(unsigned)(b > cap ? cap : b), 256, 0, qs_stream(stream)>>>(
+        n, lg, indptr, indices, (const float4 *)x, (float4 *)y);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}

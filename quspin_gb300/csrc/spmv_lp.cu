@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
     __syncthreads();
     const cx<S> av{s_a[0], s_a[1]};
     const int k2 = s_k;
+    const unsigned long long keep = l2_keep_policy();
     const BE *xc = reinterpret_cast<const BE *>(xv);
     const S *xr = reinterpret_cast<const S *>(xv);
 
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
                         for (int b = 0; b < NB; b++) {
                             if (NB == 1 || c0 + b < nvec) {
                                 const int64_t xi = (int64_t)col[u] * nvec + c0 + b;
-                                if constexpr (XC) vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(xc + xi));
+                                if constexpr (XC) vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(xc + xi, keep));
                                 else rmul_acc<M>(ar[b], ai[b], d[u], M::ldS(xr + xi));
                             }
                         }
