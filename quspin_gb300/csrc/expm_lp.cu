@@ -167,7 +167,9 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
 #pragma unroll
                         for (int b = 0; b < NB; b++)
                             if (NB == 1 || c0 + b < nvec)
-                                vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(Bin + (int64_t)col[u] * nvec + c0 + b, keep));
+                                vmul_acc<M>(ar[b], ai[b], d[u],
+                                            NB == 1 ? M::ldB(Bin + col[u], keep)
+                                                    : M::ldB(Bin + (int64_t)col[u] * nvec + c0 + b));
                     }
                 }
             }

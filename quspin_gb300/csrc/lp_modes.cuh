@@ -11,9 +11,10 @@
 namespace {
 
 // L2 eviction priority for the gathered vector (createpolicy, PTX ISA 7.4+):
-// its gathers carry an evict_last policy so that its lines outlive the
-// streamed indices, values and partial sums (loaded and stored evict-first
-// through __ldcs / __stcs) while a product or Taylor term runs.
+// single-vector gathers carry an evict_last policy so that the vector's
+// lines outlive the streamed indices, values and partial sums (loaded and
+// stored evict-first through __ldcs / __stcs) while a product or Taylor term
+// runs.  Multi-vector blocks are far larger than L2 and keep the default.
 __device__ __forceinline__ unsigned long long l2_keep_policy()
 {
     unsigned long long pol;

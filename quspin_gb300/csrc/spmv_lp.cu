@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
                         for (int b = 0; b < NB; b++) {
                             if (NB == 1 || c0 + b < nvec) {
                                 const int64_t xi = (int64_t)col[u] * nvec + c0 + b;
-                                if constexpr (XC) vmul_acc<M>(ar[b], ai[b], d[u], M::ldB(xc + xi, keep));
+                                if constexpr (XC)
+                                    vmul_acc<M>(ar[b], ai[b], d[u], NB == 1 ? M::ldB(xc + xi, keep) : M::ldB(xc + xi));
                                 else rmul_acc<M>(ar[b], ai[b], d[u], M::ldS(xr + xi));
                             }
                         }

@@ -41,6 +41,8 @@ def result_dtype(*dtypes):
 
 class DeviceCSR:
     format = "csr"
+    # products after which matvec_into switches to the coded float-pair operand
+    CODE_AFTER_PRODUCTS = 64
 
     def __init__(self, indptr, indices, data, shape, dtype):
         self.indptr = indptr
@@ -125,7 +127,12 @@ class DeviceCSR:
             group = tune_spmv(self, nvec, xt, prec)
         a = complex(a)
         if paired:
-            P = self.paired()
+            # the coded operand costs one sort of the values; build it for a
+            # matrix that has been reused (or when a Taylor operand exists)
+            P = self.__dict__.get("_paired_coded")
+            if P is None:
+                self._nprod = self.__dict__.get("_nprod", 0) + 1
+                P = self.paired(coded=self._nprod > self.CODE_AFTER_PRODUCTS)
             xs, nrm = self._pair_scratch(x.numel() * (2 if xt.kind == "c" else 1))
             _lib.call("qs_csr_matvec_pairs", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
                       D.ptr(P.data), P.vcode, D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,
@@ -282,11 +289,20 @@ class PairedCSR:
 
     def _encode(self, src):
         if self.complex:
-            uniq, inv = torch.unique(torch.view_as_real(src), dim=0, return_inverse=True)
-            if uniq.shape[0] > self.TABLE:
+            # one-dimensional sorts only: real and imaginary parts separately,
+            # then the pairs of their codes
+            ri = torch.view_as_real(src)
+            ur, cr = torch.unique(ri[:, 0], return_inverse=True)
+            ui, ci = torch.unique(ri[:, 1], return_inverse=True)
+            if ur.numel() > self.TABLE * self.TABLE or ui.numel() > self.TABLE * self.TABLE:
+                return False
+            up, inv = torch.unique(cr.to(torch.int64) * ui.numel() + ci.to(torch.int64), return_inverse=True)
+            if up.numel() > self.TABLE:
                 return False
             vals = torch.zeros(self.TABLE, 2, dtype=torch.float64, device=D.device())
-            vals[:uniq.shape[0]] = uniq
+            vals[:up.numel(), 0] = ur[up // ui.numel()]
+            vals[:up.numel(), 1] = ui[up % ui.numel()]
+            uniq = up
         else:
             uniq, inv = torch.unique(src, return_inverse=True)
             if uniq.numel() > self.TABLE:
