@@ -254,6 +254,38 @@ class DeviceDIA:
         return self.tocsr().diagonal().sum()
 
 
+def value_codes(src, table=256):
+    """The coded form of a value array: (vals, codes, distinct) with vals the
+    table padded with zeros to ``table`` entries (float64 [table], or
+    [table, 2] real / imaginary parts for complex src), codes uint8 with
+    vals[codes] == src exactly, or None when src has more than ``table``
+    distinct values (or a NaN).  Only one-dimensional sorts: complex values
+    are coded by the pair of their real- and imaginary-part codes."""
+    if src.numel() == 0 or bool(torch.isnan(torch.view_as_real(src) if src.is_complex() else src).any()):
+        return None
+    if src.is_complex():
+        ri = torch.view_as_real(src)
+        ur, cr = torch.unique(ri[:, 0], return_inverse=True)
+        ui, ci = torch.unique(ri[:, 1], return_inverse=True)
+        if ur.numel() > table * table or ui.numel() > table * table:
+            return None
+        up, inv = torch.unique(cr.to(torch.int64) * ui.numel() + ci.to(torch.int64), return_inverse=True)
+        if up.numel() > table:
+            return None
+        vals = torch.zeros(table, 2, dtype=torch.float64, device=src.device)
+        vals[:up.numel(), 0] = ur[up // ui.numel()]
+        vals[:up.numel(), 1] = ui[up % ui.numel()]
+        distinct = int(up.numel())
+    else:
+        uniq, inv = torch.unique(src, return_inverse=True)
+        if uniq.numel() > table:
+            return None
+        vals = torch.zeros(table, dtype=torch.float64, device=src.device)
+        vals[:uniq.numel()] = uniq
+        distinct = int(uniq.numel())
+    return vals, inv.reshape(-1).to(torch.uint8), distinct
+
+
 class PairedCSR:
     """A DeviceCSR whose values are kept as float pairs hi + lo, the operand
     form of the paired-single kernels (csrc/expm_lp.cu, csrc/spmv_lp.cu).
@@ -288,35 +320,18 @@ class PairedCSR:
         self.coded = False
 
     def _encode(self, src):
-        if self.complex:
-            # one-dimensional sorts only: real and imaginary parts separately,
-            # then the pairs of their codes
-            ri = torch.view_as_real(src)
-            ur, cr = torch.unique(ri[:, 0], return_inverse=True)
-            ui, ci = torch.unique(ri[:, 1], return_inverse=True)
-            if ur.numel() > self.TABLE * self.TABLE or ui.numel() > self.TABLE * self.TABLE:
-                return False
-            up, inv = torch.unique(cr.to(torch.int64) * ui.numel() + ci.to(torch.int64), return_inverse=True)
-            if up.numel() > self.TABLE:
-                return False
-            vals = torch.zeros(self.TABLE, 2, dtype=torch.float64, device=D.device())
-            vals[:up.numel(), 0] = ur[up // ui.numel()]
-            vals[:up.numel(), 1] = ui[up % ui.numel()]
-            uniq = up
-        else:
-            uniq, inv = torch.unique(src, return_inverse=True)
-            if uniq.numel() > self.TABLE:
-                return False
-            vals = torch.zeros(self.TABLE, dtype=torch.float64, device=D.device())
-            vals[:uniq.numel()] = uniq
+        coded = value_codes(src, self.TABLE)
+        if coded is None:
+            return False
+        vals, codes, distinct = coded
         count = vals.numel()
         tbytes = count * 8                       # one float pair (8 bytes) per double
         buf = torch.empty(tbytes + ((src.numel() + 15) // 16) * 16, dtype=torch.uint8, device=D.device())
         _lib.call("qs_split_pairs", count, D.ptr(vals), D.ptr(buf), D.stream())
-        buf[tbytes:tbytes + src.numel()].copy_(inv.reshape(-1).to(torch.uint8))
+        buf[tbytes:tbytes + src.numel()].copy_(codes)
         self.data = buf
         self.coded = True
-        self.distinct = int(uniq.shape[0])
+        self.distinct = distinct
         return True
 
     @property
