@@ -1,7 +1,7 @@
 """CPU oracle for the QuSpin hot path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline /
-reference leg import this module, and only as the checker or the timed CPU
+reference leg import this module, and only as the comparison or the timed CPU
 baseline.  The product package ``quspin_gb300`` never imports it.
 
 It restates, on the CPU, the reference's algorithm for every step of the hot

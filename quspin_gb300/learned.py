@@ -9,7 +9,7 @@ time-dependent evolution this runs at every step.  Here a small MLP
 ``csrc/mlp.cu``) predicts (m*, s) from cheap features of the step; it is
 trained on the GPU by the project's own forward / backward / Adam kernels on
 (feature, m*, s) tuples that the plain selection generates.  The plain
-selection stays the fallback and the judge: a step whose Taylor loop used
+selection stays the fallback and the arbiter: a step whose Taylor loop used
 all m* terms of a substep without the stopping test firing is recomputed
 with the plain (m*, s).
 """
