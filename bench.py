@@ -39,7 +39,7 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(workload="j1j2_chain_L32_Sz0_k0_p+1_z+1_expm_t5", L=32, J1=1.0, J2=0.5, t=5.0,
                 sector="Sz=0,k=0,p=+1,z=+1", state="seeded normalised complex128 Gaussian (seed 0)",
                 l2="inputs larger than L2 (every Taylor term streams the CSR operand, 0.64 GB of column indices "
-                   "plus 0.16 GB of value codes, and reads and writes the 75 MB term vectors and the 150 MB "
+                   "plus 0.16 GB of value codes, and reads and writes the 75 MB term vectors and the 75 MB "
                    "partial sum; L2 is 129 MB)")
 FALLBACK_HBM_GBS = 6800.0
 
