@@ -190,3 +190,29 @@ def test_oracle_projector_invariants():
             np.testing.assert_allclose((Ph @ P).toarray(), np.eye(ob.Ns), atol=1e-14)
             Hf = O.make_static(rowb, static, np.complex128)
             np.testing.assert_allclose((Ph @ Hf @ P).toarray(), H.toarray(), atol=1e-13)
+
+
+def test_oracle_block_decomposition_of_evolution():
+    """The identity block_ops rests on (tools/block_tools.py:618-795 in the
+    reference): a state that breaks the translation symmetry evolves as the
+    sum over momentum blocks of P_k e^{-itH_k} P_k^dagger psi.  Oracle
+    projectors and sector matrices against the full-space evolution."""
+    L = 8
+    m = chain_maps(L)
+    static = [["zz", [[1.0, i, (i + 1) % L] for i in range(L)]], ["x", [[0.7, i] for i in range(L)]]]
+    full = O.OracleBasis(L, [(0, 0, 0)], pauli=1)
+    Hf = O.make_static(full, static, np.complex128).tocsr()
+    rng = np.random.default_rng(5)
+    psi = rng.normal(size=2 ** L) + 1j * rng.normal(size=2 ** L)
+    psi /= np.linalg.norm(psi)
+    ref = expm_multiply(-1.3j * Hf, psi)
+    out = np.zeros_like(psi)
+    total = 0
+    for k in range(L):
+        b = O.OracleBasis(L, [(0, 0, 0)], pauli=1, kblock=(m["t"], k))
+        P = b.get_proj(np.complex128)
+        Hk = O.make_static(b, static, np.complex128).tocsr()
+        out += P @ expm_multiply(-1.3j * Hk, P.conj().T @ psi)
+        total += b.Ns
+    assert total == 2 ** L
+    np.testing.assert_allclose(out, ref, atol=1e-12)
