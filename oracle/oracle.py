@@ -300,6 +300,26 @@ class OracleBasis:
         dtype = np.dtype(dtype)
         return P.astype(dtype) if dtype.kind == "c" else sp.csc_matrix(P.real.astype(dtype))
 
+    def get_amp(self, states, mode="representative"):
+        """Restates basis.get_amp (base_general.py:1183-1269): the factor C with
+        psi_s = C psi^sym_r for a state s and its representative r; 0 outside
+        the sector.  'representative': states are representatives (C = sqrt(n/|G|));
+        'full_basis': states are full-basis states, C = sqrt(n_r/|G|) conj(chi(g))
+        sign(g) for the first group element g taking s to r.  Returns (C, r)."""
+        s = np.ascontiguousarray(np.atleast_1d(states), dtype=np.uint64)
+        G = int(np.prod(self.pers, dtype=np.int64)) if len(self.pers) else 1
+        if mode == "representative":
+            n = self.normalization(s).astype(np.float64)
+            return np.sqrt(n / G).astype(np.complex128), s
+        if mode != "full_basis":
+            raise ValueError("mode accepts only the values 'representative' and 'full_basis'.")
+        r, g, sg = self.representative(s)
+        n = self.normalization(r).astype(np.float64)
+        steps = np.asarray([(int(q) * (self.L // int(p))) % self.L for q, p in zip(self.qs, self.pers)], np.int64)
+        ph = (g.astype(np.int64) @ steps) % self.L if len(steps) else np.zeros(len(s), np.int64)
+        chi = self.phase_re[ph] + 1j * self.phase_im[ph]
+        return np.sqrt(n / G) * np.conj(chi) * sg, r
+
     # -- operators -------------------------------------------------------
     def _prep(self, opstr, indx, J):
         indx = list(indx)

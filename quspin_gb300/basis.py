@@ -482,6 +482,64 @@ class basis_general:
             return v_out
         return y.squeeze()
 
+    def get_amp(self, states, out=None, amps=None, mode="representative"):
+        """Amplitude factor C with psi_s = C psi^sym_r between a state s of the
+        full basis and its representative r (base_general.py:1183-1269), 0 for
+        states outside the sector.  mode 'representative': states are
+        representatives, amps (optional, symmetric-basis amplitudes) are
+        multiplied by C in place; 'full_basis': states are full-basis states
+        and are replaced in place by their representatives, amps (full-basis
+        amplitudes) are divided by C in place.  C = sqrt(n_r / |G|) for a
+        representative and sqrt(n_r / |G|) conj(chi(g)) sign(g) for the first
+        group element g taking s to r -- the projector's entry at row s."""
+        if mode not in ("representative", "full_basis"):
+            raise ValueError("mode accepts only the values 'representative' and 'full_basis'.")
+        caller = states
+        states = np.atleast_1d(np.asarray(states, order="C", dtype=self._basis_dtype))
+        shape = states.shape
+        if out is not None:
+            if shape != out.shape:
+                raise TypeError("states and out must have same shape.")
+            if out.dtype not in (np.float32, np.float64, np.complex64, np.complex128):
+                raise TypeError("out must have datatype numpy.float32, numpy.float64, numpy.complex64, or "
+                                "numpy.complex128.")
+            if not out.flags["CARRAY"]:
+                raise ValueError("out must be C-contiguous array.")
+        elif amps is not None:
+            out = np.zeros(shape, dtype=amps.dtype)
+        else:
+            out = np.zeros(shape, dtype=np.complex128)
+        flat = states.reshape(-1)
+        G = int(np.prod(self._pers, dtype=np.int64)) if len(self._pers) else 1
+        if mode == "representative":
+            n = np.atleast_1d(self.normalization(flat)).astype(np.float64)
+            C = np.sqrt(n / G).astype(np.complex128)
+        else:
+            reps, g, sg = self.representative(flat, return_g=True, return_sign=True)
+            n = np.atleast_1d(self.normalization(reps)).astype(np.float64)
+            steps = np.asarray([(int(q) * (self._L // int(p))) % self._L for q, p in zip(self._qs, self._pers)],
+                               np.int64)
+            ph = (g.astype(np.int64) @ steps) % self._L if len(steps) else np.zeros(len(flat), np.int64)
+            chi = self._phase_re[ph] + 1j * self._phase_im[ph]
+            C = np.sqrt(n / G) * np.conj(chi) * sg
+            flat[...] = reps
+            if isinstance(caller, np.ndarray) and caller.dtype == self._basis_dtype and caller.flags["C_CONTIGUOUS"]:
+                caller.reshape(-1)[...] = reps
+        C = C.reshape(shape)
+        if out.dtype.kind != "c":
+            if np.any(np.abs(C.imag) > 1.1e-15):
+                raise TypeError("attemping to use real type for complex elements.")
+            C = C.real
+        out[...] = C
+        if amps is not None:
+            if shape != amps.shape:
+                raise TypeError("states and amps must have same shape.")
+            if mode == "representative":
+                amps *= out
+            else:
+                amps /= out
+        return out.squeeze()
+
     # -- projector to the full / particle-conserving basis -------------------
     def _pcon_basis(self):
         """The same particle sector without symmetries (rows of the pcon

@@ -216,3 +216,27 @@ def test_oracle_block_decomposition_of_evolution():
         total += b.Ns
     assert total == 2 ** L
     np.testing.assert_allclose(out, ref, atol=1e-12)
+
+
+def test_oracle_get_amp_matches_projector_entries():
+    """get_amp's factor C (psi_s = C psi^sym_r) is the projector entry at row s
+    of r's column, in both modes (test/test_get_amp.py checks the same through
+    get_vec), complex momenta and fermion signs included."""
+    for N, sectors, fermion, blocks, static in _proj_cases():
+        ob = O.OracleBasis(N, sectors, fermion=fermion, pauli=0, **blocks)
+        if ob.Ns == 0:
+            continue
+        pcon = O.OracleBasis(N, sectors, fermion=fermion, pauli=0)
+        P = ob.get_proj(np.complex128, pcon_basis=pcon).tocsr()
+        # representative mode: the representatives' own rows
+        C, _ = ob.get_amp(ob.states, mode="representative")
+        rows = pcon.index(ob.states)
+        np.testing.assert_allclose(C, np.asarray(P[rows, np.arange(ob.Ns)]).ravel(), atol=1e-14)
+        # full-basis mode: every state of the particle sector
+        C, r = ob.get_amp(pcon.states, mode="full_basis")
+        col = ob.index(r)
+        inside = col >= 0
+        expect = np.zeros(pcon.Ns, np.complex128)
+        expect[inside] = np.asarray(P[np.arange(pcon.Ns)[inside], col[inside]]).ravel()
+        np.testing.assert_allclose(np.where(inside, C, 0), expect, atol=1e-14)
+        assert np.all(np.abs(C[~inside]) == 0)

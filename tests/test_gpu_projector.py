@@ -96,6 +96,52 @@ def test_get_proj_noncommuting_maps_matches_oracle():
             _same(gb.get_proj(np.complex128), ob.get_proj(np.complex128))
 
 
+def test_get_amp_matches_oracle():
+    """basis.get_amp in both modes against the oracle's restatement (whose
+    factors equal the oracle projector's entries, tests/test_cpu_oracle.py)."""
+    for kind, Np, blocks in _cases():
+        gb, ob, pb = _pair(kind, Np, blocks)
+        if gb.Ns == 0:
+            continue
+        C = gb.get_amp(gb.states.copy(), mode="representative")
+        Co, _ = ob.get_amp(ob.states, mode="representative")
+        np.testing.assert_allclose(np.atleast_1d(C), Co, rtol=0, atol=1e-15)
+        full = pb.states.astype(gb.dtype)
+        st = full.copy()
+        C = gb.get_amp(st, mode="full_basis")
+        Co, ro = ob.get_amp(pb.states, mode="full_basis")
+        np.testing.assert_allclose(np.atleast_1d(C), Co, rtol=0, atol=1e-15)
+        np.testing.assert_array_equal(st, ro.astype(gb.dtype))       # states replaced by representatives
+
+
+def test_get_amp_round_trip():
+    """test/test_get_amp.py on a 4x4 lattice sector: representative-mode
+    factors turn symmetric amplitudes into the full-basis amplitudes that
+    project_from gives; full-basis mode turns them back."""
+    Lx = Ly = 4
+    N = Lx * Ly
+    s_ = np.arange(N)
+    x, y = s_ % Lx, s_ // Lx
+    tx, ty, z = (x + 1) % Lx + Lx * y, x + Lx * ((y + 1) % Ly), -(s_ + 1)
+    for kx, ky in ((0, 0), (1, 0), (1, 2)):
+        b = spin_basis_general(N, pauli=0, Nup=N // 2, kxblock=(tx, kx), kyblock=(ty, ky), zblock=(z, 0))
+        bf = spin_basis_general(N, pauli=0, Nup=N // 2)
+        rng = np.random.default_rng(kx + 10 * ky)
+        v = rng.normal(size=b.Ns) + 1j * rng.normal(size=b.Ns)
+        v /= np.linalg.norm(v)
+        inds = bf.index(b.states)
+        psi = v.copy()
+        b.get_amp(b.states.copy(), amps=psi, mode="representative")
+        full = b.project_from(v, pcon=True, sparse=False)
+        np.testing.assert_allclose(psi, full[inds], atol=1e-14)
+        states_full = bf.states.copy()
+        amps = full.copy()
+        with np.errstate(divide="ignore", invalid="ignore"):      # states outside the sector have C = 0
+            b.get_amp(states_full, amps=amps, mode="full_basis")
+        np.testing.assert_array_equal(states_full, b.representative(bf.states))
+        np.testing.assert_allclose(amps[inds], v, atol=1e-13)
+
+
 def test_project_to_from_match_projector():
     """test/test_project_to.py: P v == project_from(v) and P^dagger v_full ==
     project_to(v_full) for the reference's list of L=12 bases."""
