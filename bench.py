@@ -24,6 +24,7 @@ streams it from HBM; no separate L2 flush is needed.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -166,6 +167,11 @@ def max_over_ranks(x, ws, device=None):
     return float(t.item())
 
 
+def workload_config(n, nnz, ws):
+    """The workload's defining parameters (the same dict in both arms)."""
+    return dict(WORKLOAD, Ns=int(n), nnz=int(nnz), parallelism="replicas" if ws > 1 else "single")
+
+
 def build_problem(L, J1, J2):
     from quspin_gb300 import hamiltonian, spin_basis_general
     b = spin_basis_general(L, Nup=L // 2, pauli=0, **chain_blocks(L))
@@ -173,11 +179,17 @@ def build_problem(L, J1, J2):
     return b, H
 
 
+def taylor_kernel_name(group):
+    """Kernel the launch code selects for one vector in the float forms."""
+    return "taylor_r32_kernel" if (group >> 20) & 3 else "taylor_lp_kernel"
+
+
 def taylor_term_bytes(n, nnz, nvec=1, vb=8):
     """Algorithmic bytes of one fused Taylor term, int32 indices, complex128
     B and F: values (vb bytes per nonzero: 8 for one float pair, 1 for a code
-    byte into the 256-entry table) and indices once, indptr once, B gathered
-    once (compulsory), new B written, F read and written."""
+    byte into the 256-entry table, 0 when the code travels inside the column
+    word) and indices once, indptr once, B gathered once (compulsory), new B
+    written, F read and written."""
     return nnz * (vb + 4) + 4 * (n + 1) + n * nvec * (16 + 16 + 2 * 16)
 
 
@@ -269,23 +281,29 @@ def time_kernels(op, F, reps=20):
 
 
 def gather_probe(A, F, reps=10):
-    """The gather-rate floor for this matrix (qs_gather_probe: the product's
-    row hand-out and its random 16-byte gathers of the vector, no values, no
+    """The gather-rate floor for this matrix (bench_gather_probe in
+    bench_probe.cu, built into _build/libqsprobe.so: the product's row
+    hand-out and its random 16-byte gathers of the vector, no values, no
     arithmetic, no epilogue), fastest of G = 2, 4, 8 lanes per row at 6 or 8
     blocks per SM.  Returns (ms, G, blocks per SM) or None."""
     import torch
-    from quspin_gb300 import _lib
     from quspin_gb300 import _device as D
-    if A.idx64:
+    path = os.path.join(ROOT, "_build", "libqsprobe.so")
+    if A.idx64 or not os.path.exists(path):
         return None
+    probe = ctypes.CDLL(path).bench_gather_probe
+    probe.restype = ctypes.c_int
     y = torch.empty_like(F)
     st = torch.cuda.current_stream()
     best = None
     for G in (2, 4, 8):
         for bps in (6, 8):
             def run():
-                _lib.call("qs_gather_probe", A.shape[0], D.ptr(A.indptr), D.ptr(A.indices), D.ptr(F), D.ptr(y), G,
-                          bps, D.stream())
+                rc = probe(ctypes.c_int64(A.shape[0]), ctypes.c_void_p(D.ptr(A.indptr)),
+                           ctypes.c_void_p(D.ptr(A.indices)), ctypes.c_void_p(D.ptr(F)), ctypes.c_void_p(D.ptr(y)),
+                           G, bps, ctypes.c_void_p(D.stream()))
+                if rc:
+                    raise RuntimeError("bench_gather_probe returned {}".format(rc))
             for _ in range(2):
                 run()
             torch.cuda.synchronize()
@@ -417,38 +435,54 @@ def library_spmv(A, F, n_bytes, reps=20):
     return out
 
 
-def cpu_baseline(H, op, terms_per_evolution, budget_s=12.0):
-    """Oracle OpenMP Taylor loop on the host cores over a bounded sample of
-    Taylor terms of this evolution; evolutions/s scaled by the executed term
-    count of the GPU run."""
-    from oracle import oracle as O
-    A = H.static.tocsr() if hasattr(H, "static") else H
-    ip, ix, dt, cp, n = O._csr_parts(A)
-    rng = np.random.default_rng(0)
-    v = rng.normal(size=n) + 1j * rng.normal(size=n)
-    v /= np.linalg.norm(v)
-    L = O.lib()
-    a = complex(op.a)
-    mu = complex(op._mu)
+class OracleEvolution:
+    """The oracle's OpenMP Taylor loop (oracle/sparse_oracle.c, the restated
+    CPU path of the reference's parallel-sparse-tools expm kernel) run one
+    substep at a time on the host cores: substep i of e^{aA} v with the real
+    coefficients a / (s (j + 1)), shift, tolerance and stopping test, the state
+    carried from substep to substep and reset to v when an evolution starts."""
 
-    def run(terms):
-        x = v.astype(np.complex128).copy()
-        w = np.zeros(2 * n, np.complex128)
-        t0 = time.perf_counter()
-        # s = 1, m* = terms, tol = 0: exactly `terms` Taylor terms
-        L.orc_expm_multiply(ip, ix, dt, cp, n, 1, 1, int(terms), 0.0, mu.real, mu.imag, a.real / 1000.0,
-                            a.imag / 1000.0, 1.0, 0.0, x.view(np.float64).reshape(-1),
-                            w.view(np.float64).reshape(-1))
-        return time.perf_counter() - t0
-    t2 = run(2)
-    k = int(max(2, min(200, budget_s / max(t2 / 2, 1e-6))))
-    tk = run(k)
-    per_term = tk / k
-    return {"value": 1.0 / (per_term * terms_per_evolution), "unit": "evolutions/s", "cores": int(O.num_threads()),
-            "kind": "port",
-            "sample": "{} fused Taylor terms of this evolution on the host (oracle OpenMP loop, {:.2f} s), scaled "
-                      "by the {} terms one GPU evolution executes".format(k, tk, terms_per_evolution),
-            "seconds_per_term": per_term}
+    def __init__(self, A, v, a, mu, s, m_star, tol):
+        from oracle import oracle as O
+        self.O = O
+        self.parts = O._csr_parts(A)
+        self.v = np.ascontiguousarray(v, dtype=np.complex128)
+        self.x = self.v.copy()
+        self.w = np.zeros(2 * self.v.size, np.complex128)
+        self.a, self.mu = complex(a), complex(mu)
+        self.s, self.m_star, self.tol = int(s), int(m_star), float(tol)
+        self.eta = np.exp(self.a * self.mu / self.s)
+        self.k = 0
+        self.terms = []
+
+    def substep(self):
+        ip, ix, dt, cp, n = self.parts
+        if self.k % self.s == 0:
+            self.x[:] = self.v
+        t = self.O.lib().orc_expm_substep(ip, ix, dt, cp, n, 1, self.s, self.m_star, self.tol, self.mu.real,
+                                          self.mu.imag, self.a.real, self.a.imag, self.eta.real, self.eta.imag,
+                                          self.x.view(np.float64).reshape(-1), self.w.view(np.float64).reshape(-1))
+        self.k += 1
+        self.terms.append(int(t))
+        return t
+
+
+def cpu_baseline(A, v, op, budget_s=12.0):
+    """The oracle's OpenMP Taylor loop on the host cores over a bounded
+    sample of the same evolution: whole substeps (real coefficients, shift,
+    tolerance and stopping test) until the budget is spent; evolutions/s =
+    substeps / s / seconds."""
+    from oracle import oracle as O
+    ev = OracleEvolution(A, v, op.a, op._mu, op.s, op.m_star, op._tol)
+    t0 = time.perf_counter()
+    while ev.k < op.s and (ev.k == 0 or time.perf_counter() - t0 < budget_s):
+        ev.substep()
+    T = time.perf_counter() - t0
+    return {"value": ev.k / op.s / T, "unit": "evolutions/s", "cores": int(O.num_threads()), "kind": "port",
+            "sample": "the first {} of the {} substeps of this evolution ({} Taylor terms, real coefficients, shift "
+                      "and stopping test) in the oracle's OpenMP loop, {:.2f} s; evolutions/s = substeps / {} / "
+                      "seconds".format(ev.k, op.s, sum(ev.terms), T, op.s),
+            "seconds_per_term": T / max(sum(ev.terms), 1)}
 
 
 def run_ours(args, rank, ws):
@@ -471,6 +505,7 @@ def run_ours(args, rank, ws):
     rng = np.random.default_rng(0)
     v = rng.normal(size=n) + 1j * rng.normal(size=n)
     v /= np.linalg.norm(v)
+    v_host = v.copy()
     v_dev = torch.tensor(v, dtype=torch.complex128, device=dev)
     F = torch.empty_like(v_dev)
     for _ in range(args.warmup):
@@ -527,7 +562,7 @@ def run_ours(args, rank, ws):
     t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8 = time_kernels(op, v_dev)
     lib_ctx = library_spmv(A, v_dev, spmv_bytes(n, nnz)) if A.dtype == np.float64 else {"unavailable": "complex"}
     peak, peak_kind = peak_hbm()
-    P = A.paired()
+    P, _ = op._operand(1)           # the operand form the evolution runs on (coded, or codes packed in the indices)
     vb = P.value_bytes
     probe = gather_probe(A, v_dev)
     tb = taylor_term_bytes(n, nnz, vb=vb)
@@ -540,9 +575,10 @@ def run_ours(args, rank, ws):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (partial sums, shift, stopping test) with f32-pair products",
         "data": "synthetic (seeded Gaussian state; Hamiltonian exactly as configured)",
-        "config": dict(W, Ns=n, nnz=nnz, m_star=op.m_star, s=op.s, terms_per_evolution=terms,
-                       parallelism="replicas" if ws > 1 else "single", build_s=round(t_build, 3),
-                       expm_setup_s=round(t_setup, 3), precision="double (float-pair products)"),
+        "config": workload_config(n, nnz, ws),
+        "expm": {"m_star": int(op.m_star), "s": int(op.s), "terms_per_evolution": int(terms),
+                 "build_s": round(t_build, 3), "expm_setup_s": round(t_setup, 3),
+                 "precision": "double (float-pair products)", "built_by": "GPU basis and CSR kernels"},
         "ieee_fp64": {"value": ws * steps_ieee / T_ieee, "unit": "evolutions/s", "taylor_term_ms": 1e3 * t_ieee,
                       "launch_shape": {"lanes_per_row": group_ieee & 0xff,
                                        "entries_in_flight": (group_ieee >> 8) & 0xff},
@@ -550,10 +586,12 @@ def run_ours(args, rank, ws):
         "e2e": {"value": ws * args.steps / T_e2e, "unit": "evolutions/s", "h2d_bytes_per_step": int(n * 16),
                 "d2h_bytes_per_step": int(n * 16)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": "taylor_lp_kernel",
+                     "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": taylor_kernel_name(group),
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
                      "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff,
-                                      "blocks_per_sm_cap": {0: None, 1: 6, 2: 8}[(group >> 18) & 3]},
+                                      "blocks_per_sm_cap": ({0: 4, 1: 6} if (group >> 20) & 3 else
+                                                            {0: None, 1: 6, 2: 8}).get((group >> 18) & 3)},
+                     "operand": "codes packed in the column words" if vb == 0 else "coded values",
                      "value_bytes_per_nonzero": vb, "distinct_values": getattr(P, "distinct", None),
                      "gathers_per_s": nnz / t_term,
                      "gather_probe": None if probe is None else {
@@ -569,7 +607,7 @@ def run_ours(args, rank, ws):
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
         try:
-            out["cpu_baseline"] = cpu_baseline(H, op, terms)
+            out["cpu_baseline"] = cpu_baseline(A.tocsr(), v_host, op)
         except Exception as e:  # report, never fake
             out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
     if rank == 0:
@@ -1001,78 +1039,60 @@ def run_evolve(args):
 
 
 def run_reference(args, rank, ws):
-    """The reference's CPU path (the oracle port of QuSpin's OpenMP basis,
-    CSR assembly and Taylor loop) on the host cores; each step a bounded
-    sample of Taylor terms of the same evolution."""
+    """The reference's CPU path for this workload, restated by the oracle (the
+    reference's OpenMP basis core, CSR assembly and Taylor kernel live in
+    packages that cannot be installed here): the basis and the canonical CSR
+    built by the oracle on the host cores, (m*, s) chosen by the oracle's
+    ExpmMultiplyParallel (fragment 3.1 with onenormest, seeded), then every
+    step one substep of the evolution e^{-iHt} v in the oracle's OpenMP
+    Taylor loop (OracleEvolution), substeps in order and the state carried
+    between them.  Nothing from the quspin_gb300 package is imported."""
     if rank != 0:
         return
     from oracle import oracle as O
     W = WORKLOAD
     L = W["L"]
     t0 = time.perf_counter()
-    built_on = "host (oracle basis and CSR assembly)"
-    terms = None
-    try:
-        import torch
-        gpu = torch.cuda.is_available()
-    except Exception:
-        gpu = False
-    if gpu:
-        # The timed path is the Taylor loop; its input matrix (bit-identical to
-        # the oracle's CSR, which the tests assert) is built on the GPU so the
-        # run stays within minutes, and (m*, s) and the executed term count come
-        # from the same selection there.  None of this is inside the timed region.
-        from quspin_gb300.tools import ExpmMultiplyParallel
-        b, H = build_problem(L, W["J1"], W["J2"])
-        A = H.tocsr()
-        np.random.seed(0)
-        gop = ExpmMultiplyParallel(H.tocsr_gpu(), a=-1j * W["t"])
-        vg = np.random.default_rng(0).normal(size=A.shape[0]) * (1 + 0j)
-        gop.dot(vg / np.linalg.norm(vg))
-        terms = gop.terms_executed
-        m_star, s_sub, mu = gop.m_star, gop.s, complex(gop._mu)
-        built_on = "GPU (untimed; the same CSR bits as the oracle's assembly)"
-    else:
-        ob = O.OracleBasis(L, [(1, L // 2, 0)], pauli=0, **chain_blocks(L))
-        A = ob.build_csr(O.consolidate_static(j1j2_static(L, W["J1"], W["J2"])), np.float64)
-        np.random.seed(0)
-        oop = O.ExpmMultiplyParallelOracle(A, a=-1j * W["t"])
-        m_star, s_sub, mu = oop._m_star, oop._s, complex(oop._mu)
+    ob = O.OracleBasis(L, [(1, L // 2, 0)], pauli=0, **chain_blocks(L))
+    A = ob.build_csr(O.consolidate_static(j1j2_static(L, W["J1"], W["J2"])), np.float64)
     t_build = time.perf_counter() - t0
     n = A.shape[0]
-    ip, ix, dt, cp, _ = O._csr_parts(A)
+    t0 = time.perf_counter()
+    np.random.seed(0)
+    oop = O.ExpmMultiplyParallelOracle(A, a=-1j * W["t"])
+    t_setup = time.perf_counter() - t0
     rng = np.random.default_rng(0)
     v = rng.normal(size=n) + 1j * rng.normal(size=n)
     v /= np.linalg.norm(v)
-    Lb = O.lib()
-    a = -1j * W["t"]
-    sample = 8
-
-    def step():
-        x = v.copy()
-        w = np.zeros(2 * n, np.complex128)
-        Lb.orc_expm_multiply(ip, ix, dt, cp, n, 1, 1, sample, 0.0, mu.real, mu.imag, a.real / 1000, a.imag / 1000,
-                             1.0, 0.0, x.view(np.float64).reshape(-1), w.view(np.float64).reshape(-1))
+    ev = OracleEvolution(A, v, -1j * W["t"], oop._mu, oop._s, oop._m_star, oop._tol)
     for _ in range(args.warmup):
-        step()
+        ev.substep()
+    ev.k = 0
+    ev.terms = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        step()
+        ev.substep()
     T = time.perf_counter() - t0
-    per_term = T / (args.steps * sample)
-    terms_bound = terms if terms else m_star * s_sub
-    value = 1.0 / (per_term * terms_bound)
+    s_sub = int(oop._s)
+    value = args.steps / s_sub / T
     out = {"metric": "expm_multiply evolutions/s", "value": value, "unit": "evolutions/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded Gaussian state; Hamiltonian exactly as configured)", "impl": "reference",
-           "config": dict(W, Ns=n, nnz=int(A.nnz), m_star=int(m_star), s=int(s_sub), build_s=round(t_build, 2),
-                          input_built_on=built_on),
+           "config": workload_config(n, int(A.nnz), ws),
+           "expm": {"m_star": int(oop._m_star), "s": s_sub, "terms_timed": int(sum(ev.terms)),
+                    "build_s": round(t_build, 2), "expm_setup_s": round(t_setup, 2),
+                    "built_by": "oracle (host cores): basis, CSR assembly and (m*, s) selection"},
            "cpu_baseline": {"value": value, "unit": "evolutions/s", "cores": int(O.num_threads()), "kind": "port",
-                            "sample": "each step = {} fused Taylor terms of the evolution (oracle OpenMP loop); "
-                                      "evolutions/s = 1 / (time per term x {} terms per evolution)".format(
-                                          sample, terms_bound)},
+                            "sample": "each step = one substep of the evolution (substeps in order, {} Taylor terms "
+                                      "over the {} timed steps; real coefficients, shift, tolerance and stopping "
+                                      "test) in the oracle's OpenMP loop; evolutions/s = steps / {} / "
+                                      "seconds".format(int(sum(ev.terms)), args.steps, s_sub)},
            "e2e": {"value": value, "unit": "evolutions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    loaded = sorted(m for m in sys.modules if m == "quspin_gb300" or m.startswith("quspin_gb300."))
+    if loaded:
+        raise RuntimeError("the reference arm imported the GPU package: {}".format(loaded))
+    out["expm"]["gpu_package_imported"] = False
     print(json.dumps(out))
 
 

@@ -8,8 +8,11 @@
 // entries in flight per lane) and no values, no arithmetic beyond the sums,
 // no epilogue.  Its time is the floor a kernel with this access pattern can
 // reach; bench.py reports the Taylor kernel's time against it.  It is a
-// measurement helper only: no product path calls it.
-#include "qs_common.cuh"
+// measurement helper of bench.py only, built into its own library
+// (_build/libqsprobe.so, by __graft_entry__.build) and never linked into
+// libqsgpu.so.
+#include <cuda_runtime.h>
+#include <stdint.h>
 
 namespace {
 
@@ -53,17 +56,19 @@ __global__ void __launch_bounds__(256) gather_probe_kernel(int64_t n, int lgG, c
 // y[r] = sum over row r of x[indices[k]] for an n-row CSR with int32 indptr
 // and indices; x, y: 16-byte elements (n of each).  G lanes per row (2, 4, 8);
 // blocks_per_sm: grid size in blocks per SM (1..16).
-extern "C" int qs_gather_probe(int64_t n, const int32_t *indptr, const int32_t *indices, const void *x, void *y,
+extern "C" int bench_gather_probe(int64_t n, const int32_t *indptr, const int32_t *indices, const void *x, void *y,
                                int G, int blocks_per_sm, void *stream)
 {
-    if (n < 1 || !indptr || !indices || !x || !y) return QS_ERR_ARG;
-    if ((G != 2 && G != 4 && G != 8) || blocks_per_sm < 1 || blocks_per_sm > 16) return QS_ERR_ARG;
+    if (n < 1 || !indptr || !indices || !x || !y) return -1;
+    if ((G != 2 && G != 4 && G != 8) || blocks_per_sm < 1 || blocks_per_sm > 16) return -1;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -2;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return -2;
     int lg = 0;
     while ((1 << lg) < G) lg++;
     const int64_t rows_pb = 256 / G;
-    const int64_t b = (n + rows_pb - 1) / rows_pb, cap = (int64_t)qs_num_sms() * blocks_per_sm;
-    gather_probe_kernel<<<(unsigned)(b > cap ? cap : b), 256, 0, qs_stream(stream)>>>(
+    const int64_t b = (n + rows_pb - 1) / rows_pb, cap = (int64_t)sms * blocks_per_sm;
+    gather_probe_kernel<<<(unsigned)(b > cap ? cap : b), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
         n, lg, indptr, indices, (const float4 *)x, (float4 *)y);
-    QS_CHECK(cudaGetLastError());
-    return QS_OK;
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }

@@ -127,13 +127,6 @@ int qs_proj_fill(void *sym, const void *d_states, const uint32_t *d_norms, int64
 int qs_proj_apply(int direction, int64_t Ns, const int64_t *d_colptr, const int64_t *d_rows, const void *d_P,
                   const void *d_x, int64_t k, void *d_y, void *stream);
 
-/* ---- measurement helper (no reference counterpart) ----------------------
- * Gather-rate probe for the roofline: y[r] = sum of x[indices[k]] over row r
- * (16-byte elements), the product kernels' row hand-out without values or
- * epilogue.  int32 indptr / indices; G in {2, 4, 8}; blocks_per_sm 1..16. */
-int qs_gather_probe(int64_t n, const int32_t *d_indptr, const int32_t *d_indices, const void *d_x, void *d_y, int G,
-                    int blocks_per_sm, void *stream);
-
 /* ---- _matvec for csr / dia (html matvec/matvec_core.html:146-201) ------- */
 int qs_csr_matvec(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                   const void *d_data, int dtype, const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re,
@@ -180,7 +173,7 @@ int qs_expm_multiply(int64_t n, int64_t nnz, const void *d_indptr, int idx64, co
                      const void *d_data, int dtype, void *d_F, int64_t nvec, int s, int m_star, double tol,
                      double mu_re, double mu_im, const void *d_coeff, const void *d_eta, const void *d_one,
                      void *d_work, int btype, void *d_ctl, int group, void *stream);
-/* The same two calls with a row-sum scratch d_rownorm of n float pairs (8n bytes): with bit 16 of group set and
+/* The same two calls with a row-sum scratch d_rownorm of n double pairs (16n bytes): with bit 16 of group set and
  * more than 8 right-hand sides, the float forms sweep the rows once per chunk of 8 vectors, so the gathered
  * slice of B stays in L2 (the many-state evolutions of hamiltonian_core.py:1472-1486 and block_tools.py:618-795
  * call the Taylor loop with such blocks). */
@@ -272,6 +265,19 @@ int qs_lanczos_reorth(int64_t n, int cplx, int nk, const double *d_Q, int64_t ld
                       double *d_scratch, void *d_ctl, void *stream);
 int qs_lanczos_lincomb(int64_t n_el, int nk, const double *d_c, int cplx_c, const double *d_Q, int64_t ldq,
                        int cplx_q, double *d_out, void *stream);
+
+/* ---- dense FP64 panels of the Lanczos tools: W[i, j] = sum_r op(Q[i, r]) X[r, j]
+ * (the Krylov matrix elements of _LTLM.py:110-126, the overlaps of _FTLM.py:95-105 and
+ * full_ortho's re-projection, _lanczos_utils.py:206-222; the reference computes them with
+ * numpy dot products).  Q [m, >= n] rows (stride ldq), X [n, >= k] C order (stride ldx) or,
+ * with xrows, [k, >= n] rows; W [m, k]; cplx: complex128 interleaved; conj: op = complex
+ * conjugate.  FP64 tensor
+ * instructions (mma.sync m8n8k4 .f64) for k > 2, FP64 FMA for k <= 2; the contraction
+ * is split over n and the partial tiles summed in a fixed order (scratch from
+ * qs_block_inner_scratch_doubles). ------------------------------------------------ */
+int64_t qs_block_inner_scratch_doubles(int64_t n, int m, int k, int cplx);
+int qs_block_inner(int64_t n, int m, int k, const double *d_Q, int64_t ldq, const double *d_X, int64_t ldx,
+                   int xrows, int cplx, int conj, double *d_W, double *d_scratch, void *stream);
 
 #ifdef __cplusplus
 }

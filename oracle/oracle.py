@@ -98,6 +98,8 @@ def lib():
                                             c.c_double, c.c_double, c.c_double, c.c_double,
                                             c.c_double, c.c_double, _f64p, _f64p]
             L.orc_expm_multiply.restype = c.c_int64
+            L.orc_expm_substep.argtypes = L.orc_expm_multiply.argtypes
+            L.orc_expm_substep.restype = c.c_int64
             L.orc_build_csr.argtypes = sym + [_f64p, _f64p, c.c_int, _i32p, _i32p, c.c_char_p, _i32p, _f64p, _i32p,
                                               _u64p, _u32p, c.c_int64, c.c_int, _i64p, _i64p, c.c_int,
                                               c.POINTER(c.c_void_p), c.POINTER(c.c_void_p),
@@ -567,13 +569,22 @@ class _LazyNormInfo:
         return np.abs(self._a) * self._A_1_norm
 
     def _linop(self):
+        """a (A - mu I) and its adjoint, the products by the OpenMP CSR
+        kernel of sparse_oracle.c (one or several columns)."""
         from scipy.sparse.linalg import LinearOperator
         if self._op is None:
-            A, a, mu = self._A, self._a, self._mu
-            AH = A.transpose().conj().tocsr()
-            self._op = LinearOperator(A.shape, dtype=self._dtype,
-                                      matvec=lambda v: a * (A.dot(v) - mu * v),
-                                      rmatvec=lambda v: np.conj(a) * (AH.dot(v) - np.conj(mu) * v))
+            A, a, mu = self._A, complex(self._a), complex(self._mu)
+            AH = sp.csr_matrix(A.transpose().conj())
+            dt = np.result_type(self._dtype, np.complex128)
+
+            def mv(M, c, m, v):
+                v = np.asarray(v)
+                y = csr_matvec(M, v)
+                return c * (y - m * v.astype(dt))
+            self._op = LinearOperator(A.shape, dtype=self._dtype, matvec=lambda v: mv(A, a, mu, v),
+                                      matmat=lambda V: mv(A, a, mu, V),
+                                      rmatvec=lambda v: mv(AH, np.conj(a), np.conj(mu), v),
+                                      rmatmat=lambda V: mv(AH, np.conj(a), np.conj(mu), V))
         return self._op
 
     def d(self, p):

@@ -149,6 +149,79 @@ static double inf_norm(const double *B, int64_t n, int64_t nvec)
 }
 
 /*
+ * Substep i of the s-substep truncated-Taylor evolution e^{aA} v
+ * (_expm_multiply_simple_core, scipy _expm_multiply.py:280-306, with the
+ * shift of expm_multiply_parallel_core.html:392-396): B = F, at most m_star
+ * terms with coefficients a / (s (j + 1)), the infinity-norm stopping test,
+ * then F = eta F.  F: [n, nvec] complex, updated in place; B, T: scratch of
+ * the same size.  Returns the number of terms executed.
+ */
+static int64_t expm_substep(const int64_t *indptr, const int32_t *indices, const double *data, int data_complex,
+                            int64_t n, int64_t nvec, const int64_t *bounds, int nt, int s, int m_star, double tol,
+                            double mu_re, double mu_im, double a_re, double a_im, double eta_re, double eta_im,
+                            double *F, double *B, double *T)
+{
+    int64_t len = 2 * n * nvec;
+    memcpy(B, F, sizeof(double) * len);
+    int64_t terms = 0;
+    double c1 = inf_norm(B, n, nvec);
+    for (int j = 0; j < m_star; j++) {
+        double den = (double)s * (double)(j + 1);
+        double cr = a_re / den, ci = a_im / den;
+        double c2 = 0.0, fn = 0.0;
+        #pragma omp parallel num_threads(nt) reduction(max:c2,fn)
+        {
+#ifdef _OPENMP
+            int t = omp_get_thread_num();
+#else
+            int t = 0;
+#endif
+            double *acc = (double *)malloc(sizeof(double) * 2 * nvec);
+            for (int64_t r = bounds[t]; r < bounds[t + 1]; r++) {
+                for (int64_t c = 0; c < nvec; c++) { acc[2 * c] = 0.0; acc[2 * c + 1] = 0.0; }
+                for (int64_t k = indptr[r]; k < indptr[r + 1]; k++) {
+                    int64_t col = indices[k];
+                    double dr = data_complex ? data[2 * k] : data[k];
+                    double di = data_complex ? data[2 * k + 1] : 0.0;
+                    const double *xp = B + 2 * col * nvec;
+                    for (int64_t c = 0; c < nvec; c++) {
+                        acc[2 * c] += dr * xp[2 * c] - di * xp[2 * c + 1];
+                        acc[2 * c + 1] += dr * xp[2 * c + 1] + di * xp[2 * c];
+                    }
+                }
+                double rs_b = 0.0, rs_f = 0.0;
+                for (int64_t c = 0; c < nvec; c++) {
+                    int64_t o = 2 * (r * nvec + c);
+                    /* (A B - mu B) */
+                    double wr = acc[2 * c] - (mu_re * B[o] - mu_im * B[o + 1]);
+                    double wi = acc[2 * c + 1] - (mu_re * B[o + 1] + mu_im * B[o]);
+                    double br = cr * wr - ci * wi;
+                    double bi = cr * wi + ci * wr;
+                    T[o] = br; T[o + 1] = bi;
+                    F[o] += br; F[o + 1] += bi;
+                    rs_b += hypot(br, bi);
+                    rs_f += hypot(F[o], F[o + 1]);
+                }
+                if (rs_b > c2) c2 = rs_b;
+                if (rs_f > fn) fn = rs_f;
+            }
+            free(acc);
+        }
+        double *sw = B; B = T; T = sw;
+        terms++;
+        if (c1 + c2 <= tol * fn) break;
+        c1 = c2;
+    }
+    #pragma omp parallel for
+    for (int64_t o = 0; o < len; o += 2) {
+        double fr = F[o], fi = F[o + 1];
+        F[o] = eta_re * fr - eta_im * fi;
+        F[o + 1] = eta_re * fi + eta_im * fr;
+    }
+    return terms;
+}
+
+/*
  * In-place e^{aA} v (v: [n, nvec] complex), work: 2*n*nvec complex.
  * Returns the number of Taylor terms executed (for the error statement).
  */
@@ -163,67 +236,31 @@ int64_t orc_expm_multiply(const int64_t *indptr, const int32_t *indices, const d
     int64_t *bounds = (int64_t *)malloc(sizeof(int64_t) * (nt + 1));
     nnz_partition(indptr, n, nt, bounds);
     int64_t len = 2 * n * nvec;
-    double *B = work, *T = work + len;
-    double *F = v;
-    memcpy(B, F, sizeof(double) * len);
     int64_t terms = 0;
-    for (int i = 0; i < s; i++) {
-        double c1 = inf_norm(B, n, nvec);
-        for (int j = 0; j < m_star; j++) {
-            double den = (double)s * (double)(j + 1);
-            double cr = a_re / den, ci = a_im / den;
-            double c2 = 0.0, fn = 0.0;
-            #pragma omp parallel num_threads(nt) reduction(max:c2,fn)
-            {
-#ifdef _OPENMP
-                int t = omp_get_thread_num();
-#else
-                int t = 0;
-#endif
-                double *acc = (double *)malloc(sizeof(double) * 2 * nvec);
-                for (int64_t r = bounds[t]; r < bounds[t + 1]; r++) {
-                    for (int64_t c = 0; c < nvec; c++) { acc[2 * c] = 0.0; acc[2 * c + 1] = 0.0; }
-                    for (int64_t k = indptr[r]; k < indptr[r + 1]; k++) {
-                        int64_t col = indices[k];
-                        double dr = data_complex ? data[2 * k] : data[k];
-                        double di = data_complex ? data[2 * k + 1] : 0.0;
-                        const double *xp = B + 2 * col * nvec;
-                        for (int64_t c = 0; c < nvec; c++) {
-                            acc[2 * c] += dr * xp[2 * c] - di * xp[2 * c + 1];
-                            acc[2 * c + 1] += dr * xp[2 * c + 1] + di * xp[2 * c];
-                        }
-                    }
-                    double rs_b = 0.0, rs_f = 0.0;
-                    for (int64_t c = 0; c < nvec; c++) {
-                        int64_t o = 2 * (r * nvec + c);
-                        /* (A B - mu B) */
-                        double wr = acc[2 * c] - (mu_re * B[o] - mu_im * B[o + 1]);
-                        double wi = acc[2 * c + 1] - (mu_re * B[o + 1] + mu_im * B[o]);
-                        double br = cr * wr - ci * wi;
-                        double bi = cr * wi + ci * wr;
-                        T[o] = br; T[o + 1] = bi;
-                        F[o] += br; F[o + 1] += bi;
-                        rs_b += hypot(br, bi);
-                        rs_f += hypot(F[o], F[o + 1]);
-                    }
-                    if (rs_b > c2) c2 = rs_b;
-                    if (rs_f > fn) fn = rs_f;
-                }
-                free(acc);
-            }
-            double *sw = B; B = T; T = sw;
-            terms++;
-            if (c1 + c2 <= tol * fn) break;
-            c1 = c2;
-        }
-        #pragma omp parallel for
-        for (int64_t o = 0; o < len; o += 2) {
-            double fr = F[o], fi = F[o + 1];
-            F[o] = eta_re * fr - eta_im * fi;
-            F[o + 1] = eta_re * fi + eta_im * fr;
-            B[o] = F[o]; B[o + 1] = F[o + 1];
-        }
-    }
+    for (int i = 0; i < s; i++)
+        terms += expm_substep(indptr, indices, data, data_complex, n, nvec, bounds, nt, s, m_star, tol, mu_re, mu_im,
+                              a_re, a_im, eta_re, eta_im, v, work, work + len);
+    free(bounds);
+    return terms;
+}
+
+/*
+ * One substep of the s-substep evolution (the body of orc_expm_multiply's
+ * loop) on v in place; work: 2*n*nvec complex.  Returns the terms executed.
+ */
+int64_t orc_expm_substep(const int64_t *indptr, const int32_t *indices, const double *data,
+                         int data_complex, int64_t n, int64_t nvec,
+                         int s, int m_star, double tol,
+                         double mu_re, double mu_im, double a_re, double a_im,
+                         double eta_re, double eta_im,
+                         double *v, double *work)
+{
+    int nt = nthreads();
+    int64_t *bounds = (int64_t *)malloc(sizeof(int64_t) * (nt + 1));
+    nnz_partition(indptr, n, nt, bounds);
+    int64_t len = 2 * n * nvec;
+    int64_t terms = expm_substep(indptr, indices, data, data_complex, n, nvec, bounds, nt, s, m_star, tol, mu_re,
+                                 mu_im, a_re, a_im, eta_re, eta_im, v, work, work + len);
     free(bounds);
     return terms;
 }

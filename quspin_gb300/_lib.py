@@ -18,7 +18,7 @@ _lib = None
 _lock = threading.Lock()
 
 # element type codes shared with the C side
-F32, F64, C64, C128, PF, CPF, PF8, CPF8 = 0, 1, 2, 3, 4, 5, 6, 7
+F32, F64, C64, C128, PF, CPF, PF8, CPF8, PF8P, CPF8P = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
 
 STATUS = {
     -1: "invalid argument",
@@ -63,7 +63,6 @@ _SIGS = {
     "qs_proj_fill": (_i, [_vp, _vp, _vp, _i64, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp,
                           _vp]),
     "qs_proj_apply": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _i64, _vp, _vp]),
-    "qs_gather_probe": (_i, [_i64, _vp, _vp, _vp, _vp, _i, _i, _vp]),
     "qs_csr_matvec": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp]),
     "qs_csr_matvec_pairs": (_i, [_i64, _i64, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i64, _d, _d, _i, _i, _vp, _vp,
                                  _vp]),
@@ -112,6 +111,8 @@ _SIGS = {
     "qs_lanczos_beta": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _d, _i, _vp, _vp, _vp]),
     "qs_lanczos_reorth": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i, _vp, _vp, _vp]),
     "qs_lanczos_lincomb": (_i, [_i64, _i, _vp, _i, _vp, _i64, _i, _vp, _vp]),
+    "qs_block_inner_scratch_doubles": (_i64, [_i64, _i, _i, _i]),
+    "qs_block_inner": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i64, _i, _i, _i, _vp, _vp, _vp]),
 }
 
 

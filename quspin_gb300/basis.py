@@ -37,27 +37,50 @@ class GeneralBasisWarning(Warning):
 
 
 def process_map(map, q):
-    """Periodicity of a site map (base_general.py:22-51)."""
+    """Period of a symmetry map, with the reference's outputs and messages
+    (src/quspin/basis/basis_general/base_general.py:22-51).
+
+    ``map[i] = j >= 0`` sends site i to site j; ``map[i] = -(j + 1)`` sends it
+    to site j and inverts it (spin inversion / particle-hole).  The map is a
+    signed permutation g; its period is the order of g: along each cycle of
+    the underlying permutation, a site comes back to itself after the cycle
+    length l with the product of the inversions met on the way, so the cycle
+    contributes l when it holds an even number of inverted sites and 2 l
+    otherwise, and the period is the least common multiple of these.
+
+    Returns (map as int32, period, q, set of the powers g^k, k = 0 .. period,
+    each written as the tuple of signed site labels in the reference's
+    notation)."""
     map = np.asarray(map, dtype=np.int32)
-    i_map = map.copy()
-    i_map[map < 0] = -(i_map[map < 0] + 1)
-    s_map = map < 0
-    sites = np.arange(len(map), dtype=np.int32)
-    order = sites.copy()
-    if np.any(np.sort(i_map) - order):
+    inv = map < 0
+    dest = np.where(inv, -map - 1, map).astype(np.int64)
+    n = dest.size
+    if not np.array_equal(np.sort(dest), np.arange(n)):
         raise ValueError("map must be a one-to-one site mapping.")
-    per = 0
-    group = [tuple(order)]
-    while True:
-        sites[s_map] = -(sites[s_map] + 1)
-        sites = sites[i_map]
-        per += 1
-        group.append(tuple(sites))
-        if np.array_equal(order, sites):
-            break
+    per = 1
+    seen = np.zeros(n, dtype=bool)
+    for start in range(n):
+        if seen[start]:
+            continue
+        length, flips, i = 0, 0, start
+        while not seen[i]:
+            seen[i] = True
+            flips += int(inv[i])
+            i = int(dest[i])
+            length += 1
+        cyc = length if flips % 2 == 0 else 2 * length
+        per = per * cyc // gcd(per, cyc)
     if per == 1:
         warnings.warn("identity mapping found in set of transformations.", GeneralBasisWarning, stacklevel=5)
-    return map, per, q, set(group)
+    # powers of g: position i of g^(k+1) holds the label of position dest[i]
+    # of g^k, inverted once more when that site is an inverted one
+    label = np.arange(n, dtype=np.int64)
+    odd = np.zeros(n, dtype=bool)
+    powers = set()
+    for _ in range(per + 1):
+        powers.add(tuple(int(x) for x in np.where(odd, -label - 1, label)))
+        label, odd = label[dest], odd[dest] ^ inv[dest]
+    return map, per, q, powers
 
 
 def _phase_tables(L):

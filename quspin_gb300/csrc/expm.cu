@@ -293,7 +293,11 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // G | (U << 8) | (C << 16) (G lanes per row 2..32, U = 1, 2, 4 entries in flight
 // per lane; C = 1 asks the float forms for the chunk-outer sweep, which takes
 // effect only through qs_taylor_term_rows with a row-sum scratch; bit 17
-// narrows its chunks from 8 to 4 vectors);
+// narrows its chunks from 8 to 4 vectors; bits 18-19 cap the registers of the
+// single-vector float-pair shapes for 6 / 8 blocks per SM; bits 20-21 = 1..3
+// select the staged single-vector kernel of csrc/expm_st.cu with unit shape
+// 1: 4 lanes x 8 rows, 2: 4 lanes x 16 rows, 3: 2 lanes x 16 rows -- one
+// vector, int32 indices, 16-byte aligned index and value arrays);
 // 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                                    const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
@@ -309,7 +313,7 @@ extern "C" int qs_taylor_term(int64_t n, int64_t nnz, const void *indptr, int id
                                coeff, j, tol, ctl, group, nullptr, stream);
 }
 
-// qs_taylor_term with row-sum scratch: with rownorm (n float pairs) and the
+// qs_taylor_term with row-sum scratch: with rownorm (n double pairs) and the
 // chunk bit of group set (1 << 16), the float forms sweep the rows once per
 // vector chunk of 8 so the gathered slice of B can stay in L2.
 extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
@@ -333,6 +337,9 @@ extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, i
         LpTerm a{n, indptr, idx64, indices, data, dtype, Bin, Bout, btype, Fp, nvec, mu, nullptr, nullptr, cf, j, tol,
                  ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
         a.occ = group > 0 ? (group >> 18) & 3 : 0;
+        a.nnz = nnz;
+        a.staged = group > 0 ? (group >> 20) & 3 : 0;
+        if (a.staged) return st_taylor_term(a);
         return lp_taylor_term(a, false);
     }
     if (btype == QS_C128) {

@@ -12,6 +12,8 @@ struct ExpmCtl {
     long long terms;           // Taylor terms executed so far
     int nonconv;               // substeps that used all m* terms without the test firing
     int bexp;                  // B is stored scaled by 2^-bexp (paired / single-precision storage)
+    int err;                   // nonzero: a bounded device wait gave up (staged term kernel)
+    int pad_;
 };
 
 // block-wide max of two non-negative doubles, atomically folded into ctl
@@ -119,10 +121,15 @@ struct LpTerm {
     int G, U;
     int chunk_outer;          // sweep rows once per NB-wide vector chunk (needs rownorm)
     int narrow;               // chunk-outer with 4-vector chunks instead of 8
-    void *rownorm;            // n float pairs of row-sum scratch for chunk_outer, or null
+    void *rownorm;            // n double pairs of row-sum scratch for chunk_outer, or null
     cudaStream_t st;
     int occ = 0;              // single-vector float-pair shapes: 1 / 2 cap registers for 6 / 8 blocks per SM
+    int64_t nnz = 0;          // stored entries (the staged kernel's copy bounds)
+    int staged = 0;           // 1..3: staged single-vector kernel (csrc/expm_st.cu) with unit shape 1..3
 };
+
+// The staged single-vector term (csrc/expm_st.cu).
+int st_taylor_term(const LpTerm &a);
 
 int lp_taylor_term(const LpTerm &a, bool multi);
 // F = eta F, norms, scale exponent, then B0 = F 2^-bexp in btype storage.

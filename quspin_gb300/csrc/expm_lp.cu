@@ -27,8 +27,10 @@
 // lane holds the row sum, lanes 0 and 1 write the real and imaginary part of
 // the new term and of F (two FP64 adds each for the paired form), so the
 // FP64 pipe sees a handful of fully used instructions per row instead of
-// two per nonzero.  Row norms for the stopping test are taken in FP32 from
-// the scaled values.
+// two per nonzero.  The stopping test is evaluated on IEEE double values: the
+// squared modulus of each new term element and each F element is formed in
+// FP64 from the exact double value of the float pair (the many-vector row
+// sums of moduli take the square root with sqrt_newton).
 #include "qs_common.cuh"
 #include <type_traits>
 #include "expm_ctl.cuh"
@@ -50,7 +52,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                                                         int64_t nvec, cdbl mu0, const cdbl *__restrict__ mus,
                                                         const int64_t *__restrict__ sec_off,
                                                         const cdbl *__restrict__ coeff, int j, double tol, void *ctlp,
-                                                        float2 *__restrict__ rownorm)
+                                                        double2 *__restrict__ rownorm)
 {
     using S = typename M::S;
     using BE = typename M::BE;
@@ -60,7 +62,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
     __shared__ int s_bexp[NS];
     __shared__ int s_done[NS];
     __shared__ int64_t s_off[NS + 1];
-    __shared__ unsigned int s_mb[NS], s_mf[NS];
+    __shared__ unsigned long long s_mb[NS], s_mf[NS];
     int nsec = 1;
     if constexpr (!MULTI) {
         ExpmCtl *ctl = reinterpret_cast<ExpmCtl *>(ctlp);
@@ -87,8 +89,8 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
             const cx<S> m{M::from_d(md.x), M::from_d(md.y)};
             s_cm[2 * b] = M::sub(M::mul(c.re, m.re), M::mul(c.im, m.im));
             s_cm[2 * b + 1] = M::add(M::mul(c.re, m.im), M::mul(c.im, m.re));
-            s_mb[b] = 0u;
-            s_mf[b] = 0u;
+            s_mb[b] = 0ull;
+            s_mf[b] = 0ull;
         }
     }
     if (threadIdx.x == 32) s_cf[0] = M::from_d(coeff[j].x);
@@ -114,7 +116,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
     //   im: cf.re acc.im + cf.im acc.re - (cm.re bo.im + cm.im bo.re)
     const S cf_re = s_cf[0];
     const S cf_x = comp ? s_cf[1] : M::neg(s_cf[1]);
-    float mb = 0.f, mf = 0.f;
+    double mb = 0.0, mf = 0.0;
     // Chunk-outer order (rownorm given, several NB-wide vector chunks): the
     // whole grid sweeps the rows once per chunk, so the gathered slice of B
     // is NB columns wide and can stay in L2 across the sweep; the row sums
@@ -137,9 +139,10 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         const bool writer = valid && lane < 2;
         const IT k0 = valid ? indptr[r] : (IT)0, k1 = valid ? indptr[r + 1] : (IT)0;
         const int bexp = s_bexp[sec];
+        const double s_inv = pow2(-bexp);
         const S cm_re = s_cm[2 * sec];
         const S cm_x = comp ? s_cm[2 * sec + 1] : M::neg(s_cm[2 * sec + 1]);
-        float rbn = 0.f, rfn = 0.f;
+        double rbn = 0.0, rfn = 0.0;
         BE bo_pre{M::zero(), M::zero()};
         double f_pre = 0.0;
         if (NB == 1 && writer) {
@@ -190,30 +193,31 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                 const S bo_c = comp ? bo.im : bo.re, bo_o = comp ? bo.re : bo.im;
                 const S mine = M::sub(M::add(M::mul(cf_re, acc_c), M::mul(cf_x, acc_o)),
                                       M::add(M::mul(cm_re, bo_c), M::mul(cm_x, bo_o)));
-                float nb2 = M::hi(mine) * M::hi(mine);
-                nb2 += __shfl_xor_sync(0xffffffffu, nb2, 1);
-                float fc = 0.f;
+                // squared moduli in FP64, scaled by 2^-bexp
+                double md = 0.0, fs = 0.0;
                 if (writer) {
                     M::st_comp(Bout + e, comp, mine);
                     double *fp = reinterpret_cast<double *>(F + e) + comp;
                     double fv = NB == 1 ? f_pre : __ldcs(fp);
                     fv = M::add_to(fv, mine, bexp);
                     __stcs(fp, fv);
-                    fc = d2f_scaled(fv, bexp);
+                    md = M::to_d(mine, 0);
+                    fs = fv * s_inv;
                 }
-                float f2 = fc * fc;
-                f2 += __shfl_xor_sync(0xffffffffu, f2, 1);
+                double nb2 = __dmul_rn(md, md), f2 = __dmul_rn(fs, fs);
+                nb2 = __dadd_rn(nb2, __shfl_xor_sync(0xffffffffu, nb2, 1));
+                f2 = __dadd_rn(f2, __shfl_xor_sync(0xffffffffu, f2, 1));
                 if (NB == 1) {
                     rbn = nb2;          // one column: squared moduli, square root once at the end
                     rfn = f2;
                 } else {
-                    rbn += sqrtf(nb2);
-                    rfn += sqrtf(f2);
+                    rbn += sqrt_newton(nb2);
+                    rfn += sqrt_newton(f2);
                 }
             }
         }
         if (chunk_outer && writer && lane == 0) {
-            float2 acc = sw == 0 ? make_float2(0.f, 0.f) : rownorm[r];
+            double2 acc = sw == 0 ? make_double2(0.0, 0.0) : rownorm[r];
             acc.x += rbn;
             acc.y += rfn;
             if (sw + 1 < sweeps) rownorm[r] = acc;
@@ -223,8 +227,8 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         if (writer && sw + 1 == sweeps) {
             if constexpr (MULTI) {
                 if (lane == 0) {
-                    atomicMax(&s_mb[sec], __float_as_uint(rbn));
-                    atomicMax(&s_mf[sec], __float_as_uint(rfn));
+                    atomicMax(&s_mb[sec], (unsigned long long)__double_as_longlong(rbn));
+                    atomicMax(&s_mf[sec], (unsigned long long)__double_as_longlong(rfn));
                 }
             } else {
                 mb = fmaxf(mb, rbn);
@@ -236,7 +240,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
 
     if constexpr (!MULTI) {
         ExpmCtl *ctl = reinterpret_cast<ExpmCtl *>(ctlp);
-        fold_max2(f2d_scaled(mb, 0), f2d_scaled(mf, 0), &ctl->c2, &ctl->fn);
+        fold_max2(mb, mf, &ctl->c2, &ctl->fn);
         if (last_block(ctl) && threadIdx.x == 0) {
             volatile ExpmCtl *vc = ctl;
             double c2 = __longlong_as_double((long long)vc->c2);
@@ -257,8 +261,8 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         MultiCtl *ctl = reinterpret_cast<MultiCtl *>(ctlp);
         __syncthreads();
         for (int b = threadIdx.x; b < nsec; b += blockDim.x) {
-            if (s_mb[b]) atomicMax(&ctl->c2[b], (unsigned long long)__double_as_longlong(f2d_scaled(__uint_as_float(s_mb[b]), 0)));
-            if (s_mf[b]) atomicMax(&ctl->fn[b], (unsigned long long)__double_as_longlong(f2d_scaled(__uint_as_float(s_mf[b]), 0)));
+            if (s_mb[b]) atomicMax(&ctl->c2[b], s_mb[b]);
+            if (s_mf[b]) atomicMax(&ctl->fn[b], s_mf[b]);
         }
         if (last_block_multi(ctl) && threadIdx.x == 0) {
             volatile MultiCtl *vc = ctl;
@@ -289,7 +293,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         const DV *__restrict__ data, const typename M::BE *__restrict__ Bin, typename M::BE *__restrict__ Bout, \
         cdbl *__restrict__ F, int64_t nvec, cdbl mu0, const cdbl *__restrict__ mus,                           \
         const int64_t *__restrict__ sec_off, const cdbl *__restrict__ coeff, int j, double tol, void *ctlp, \
-        float2 *__restrict__ rownorm
+        double2 *__restrict__ rownorm
 #define TAYLOR_LP_ARGS n, lgG, indptr, indices, data, Bin, Bout, F, nvec, mu0, mus, sec_off, coeff, j, tol, ctlp, rownorm
 
 template <class M, class DV, class IT, int NB, int U, bool MULTI, bool CODED>
@@ -439,7 +443,7 @@ int lp_go(const LpTerm &a)
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
     const int blocks = taylor_grid(a.n, a.G);
-    float2 *rn = a.chunk_outer ? (float2 *)a.rownorm : nullptr;
+    double2 *rn = a.chunk_outer ? (double2 *)a.rownorm : nullptr;
     if constexpr (NB == 1 && U <= 2 && sizeof(IT) == 4 && std::is_same<M, ModePF>::value) {
         if (a.occ == 1 || a.occ == 2) {
             auto k = a.occ == 1 ? taylor_lp_kernel_occ6<M, DV, IT, NB, U, MULTI, CODED>

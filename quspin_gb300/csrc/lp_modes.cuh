@@ -162,4 +162,28 @@ __device__ __forceinline__ double pow2(int k)   // 2^k for |k| <= 1000
     return __hiloint2double((1023 + k) << 20, 0);
 }
 
+// Square root of a double for the stopping-test norms of the many-vector
+// terms, with FP64 accuracy at a few FP64 instructions: x = m 4^k with m in
+// [1, 4) (exact exponent arithmetic), y0 ~ 1/sqrt(m) from the FP32
+// reciprocal square root, one Newton-Raphson step y1 = y0 (3 - m y0^2) / 2 for
+// 1/sqrt(m) (relative error about 2^-44), s = m y1 and one Newton step for
+// the root itself, s + y1 (m - s^2) / 2, which squares the error again, so
+// the result is within a few ulps of sqrt(x).  0 for x <= 0 or NaN; x = inf
+// gives inf.
+__device__ __forceinline__ double sqrt_newton(double x)
+{
+    if (!(x > 0.0)) return 0.0;
+    const int hi = __double2hiint(x);
+    const int E = (hi >> 20) & 0x7ff;
+    if (E == 0x7ff) return x;
+    if (E == 0) return sqrt_newton(x * 0x1p104) * 0x1p-52;   // subnormal: scale into the normal range
+    const int k = (E - 1023) >> 1;                          // floor((E - 1023) / 2)
+    const double m = __hiloint2double(hi - (k << 21), __double2loint(x));   // x 4^-k, in [1, 4)
+    const double y0 = (double)rsqrtf((float)m);
+    const double y1 = y0 * fma(-0.5 * m, y0 * y0, 1.5);
+    double s = m * y1;
+    s = fma(0.5 * y1, fma(-s, s, m), s);
+    return s * __hiloint2double((1023 + k) << 20, 0);
+}
+
 }  // namespace

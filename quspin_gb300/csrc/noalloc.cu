@@ -18,6 +18,7 @@
 // control block and rewrites the coefficients before it uses them.
 #include "qs_common.cuh"
 #include <complex>
+#include <mutex>
 
 // Largest state block n * nvec (complex128 elements) the scratch can hold.
 #define QS_NOALLOC_MAX_ELEMS ((int64_t)1 << 20)
@@ -62,21 +63,27 @@ __global__ void noalloc_prepare(unsigned char *scratch, double a_re, double a_im
 
 #define QS_NOALLOC_MAX_DEVICES 64
 static void *g_noalloc_ptr[QS_NOALLOC_MAX_DEVICES];
+static cudaError_t g_noalloc_err[QS_NOALLOC_MAX_DEVICES];
+static std::once_flag g_noalloc_once[QS_NOALLOC_MAX_DEVICES];
 
 // Device address of the scratch array for the current device, looked up once
-// per device (the first call on a device does this set-up; make that first
-// call before capturing work on the stream).
+// per device with that device current (the first call on a device does this
+// set-up; make that first call before capturing work on the stream).  The
+// look-up runs under std::call_once, so host threads that make their first
+// calls at the same time wait for one look-up.  The cached address belongs to
+// the device's primary context: after cudaDeviceReset (or any reset of that
+// context) reload the library before calling again.
 static int noalloc_scratch(unsigned char **out)
 {
     int dev = 0;
     QS_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= QS_NOALLOC_MAX_DEVICES) return QS_ERR_UNSUPPORTED;
-    if (!g_noalloc_ptr[dev]) {
+    std::call_once(g_noalloc_once[dev], [dev] {
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return QS_ERR_CUDA;
-        g_noalloc_ptr[dev] = p;
-    }
+        g_noalloc_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        g_noalloc_ptr[dev] = g_noalloc_err[dev] == cudaSuccess ? p : nullptr;
+    });
+    if (g_noalloc_err[dev] != cudaSuccess || !g_noalloc_ptr[dev]) return QS_ERR_CUDA;
     *out = reinterpret_cast<unsigned char *>(g_noalloc_ptr[dev]);
     return QS_OK;
 }

@@ -334,6 +334,17 @@ class PairedCSR:
         self.distinct = distinct
         return True
 
+    def packed(self):
+        """The PackedCodedCSR form of this coded operand (cached), or None
+        when it does not apply (plain values, int64 indices, >= 2^23 columns)."""
+        if not self.coded or self.idx64 or self.shape[1] >= PackedCodedCSR.MAX_COLS:
+            return None
+        p = self.__dict__.get("_packed")
+        if p is None:
+            p = PackedCodedCSR(self)
+            self._packed = p
+        return p
+
     @property
     def nnz(self):
         return self._nnz
@@ -358,6 +369,45 @@ class PairedCSR:
             return
         count = src.numel() * (2 if self.complex else 1)
         _lib.call("qs_split_pairs", count, D.ptr(src), D.ptr(self.data), D.stream())
+
+
+class PackedCodedCSR:
+    """A coded PairedCSR with each nonzero's code byte packed into the low 8
+    bits of its column word (col << 8 | code, type codes PF8P / CPF8P): the
+    single-vector Taylor term (csrc/expm_st.cu) then reads one 4-byte word
+    per nonzero instead of a 4-byte index and a 1-byte code.  ``data`` holds
+    the 256-entry pair table only.  Needs fewer than 2^23 columns and int32
+    indices; built from a coded PairedCSR (``PairedCSR.packed()``)."""
+
+    format = "csr"
+    MAX_COLS = 1 << 23
+
+    def __init__(self, P):
+        if not P.coded or P.idx64 or P.shape[1] >= self.MAX_COLS:
+            raise ValueError("the packed form needs a coded operand with int32 indices and < 2^23 columns")
+        self.indptr, self.shape, self.idx64 = P.indptr, P.shape, 0
+        self._nnz = P.nnz
+        self.complex, self.dtype, self.distinct = P.complex, P.dtype, P.distinct
+        tbytes = PairedCSR.TABLE * (16 if P.complex else 8)
+        nnz = P.nnz
+        codes = P.data[tbytes:tbytes + nnz].to(torch.int32)
+        self.indices = torch.bitwise_or(torch.bitwise_left_shift(P.indices[:nnz].to(torch.int32), 8), codes)
+        del codes
+        self.data = P.data[:tbytes].clone()
+        self.coded = True
+
+    @property
+    def nnz(self):
+        return self._nnz
+
+    @property
+    def vcode(self):
+        return _lib.CPF8P if self.complex else _lib.PF8P
+
+    @property
+    def value_bytes(self):
+        """Bytes of value stream per nonzero beyond the 4-byte column word."""
+        return 0
 
 
 def to_device_matrix(A, dtype=None):

@@ -140,7 +140,7 @@ class DrivenEvolution:
         k = max(m, 1)
         op, bt, group = self._operand(M)
         if "_rown" not in self.__dict__:
-            self._rown = torch.empty(2 * self.n, dtype=torch.float32, device=D.device())
+            self._rown = torch.empty(2 * self.n, dtype=torch.float64, device=D.device())
         rown = self._rown if (bt != _lib.C128 and self.nvec > 8) else None
         _lib.call("qs_expm_multiply_rows", self.n, op.nnz, D.ptr(op.indptr), op.idx64, D.ptr(op.indices),
                   D.ptr(op.data), op.vcode, D.ptr(F), self.nvec, int(s), int(m), float(np.finfo(np.float64).eps / 2),

@@ -175,13 +175,33 @@ class ExpmMultiplyParallel:
             self._mixed = A.astype(vt)
         return self._mixed
 
-    def _operand(self):
-        """(matrix in the value form of the precision, B storage code)."""
+    def _operand(self, nvec=1):
+        """(matrix in the value form of the precision, B storage code).  For
+        one vector in the float-pair form, the coded operand and its packed
+        form (code bytes inside the column words) are both tuned once and the
+        faster is kept."""
         if self._precision == "mixed":
             return self._mixed_matrix(), _lib.C64
         if self._precision == "ieee":
             return self._Ad, _lib.C128
-        return self._Ad.paired(), _lib.CPF
+        P = self._Ad.paired()
+        if nvec != 1:
+            return P, _lib.CPF
+        pick = self.__dict__.get("_pick")
+        if pick is None:
+            pick = P
+            Pk = P.packed() if P.shape[0] >= 65536 else None
+            if Pk is not None:
+                from ..tune import tune_taylor
+                tune_taylor(P, 1, _lib.CPF)
+                tune_taylor(Pk, 1, _lib.CPF)
+                key = ("taylor", 1, _lib.CPF)
+                t_plain = P.__dict__.get("_tuned_ms", {}).get(key)
+                t_pack = Pk.__dict__.get("_tuned_ms", {}).get(key)
+                if t_pack is not None and t_plain is not None and t_pack < t_plain:
+                    pick = Pk
+            self._pick = pick
+        return pick, _lib.CPF
 
     def _buffers(self, n, nvec, btype):
         key = (n, nvec, btype)
@@ -196,10 +216,10 @@ class ExpmMultiplyParallel:
         return b
 
     def _rownorm(self, n):
-        """Row-sum scratch (n float pairs) of the chunk-outer Taylor sweep."""
+        """Row-sum scratch (n double pairs) of the chunk-outer Taylor sweep."""
         r = self.__dict__.get("_rown")
         if r is None or r.numel() < 2 * n:
-            r = torch.empty(max(2 * n, 2), dtype=torch.float32, device=D.device())
+            r = torch.empty(max(2 * n, 2), dtype=torch.float64, device=D.device())
             self._rown = r
         return r
 
@@ -216,7 +236,7 @@ class ExpmMultiplyParallel:
         if (work is None and n * nvec <= self.GRAPH_MAX_ELEMS and F.is_contiguous()
                 and not torch.cuda.is_current_stream_capturing()):
             return self._run_graph(F, tol)
-        M, btype = self._operand()
+        M, btype = self._operand(nvec)
         wbuf, ctl = self._buffers(n, nvec, btype)
         if work is not None and btype != _lib.C64:
             wbuf = work          # 16-byte elements: the caller's complex128 work array holds both B buffers
@@ -240,7 +260,7 @@ class ExpmMultiplyParallel:
         nvec = 1 if F.dim() == 1 else F.shape[1]
         mu = complex(self._mu)
         s, m = int(self._s), int(self._m_star)
-        M, btype = self._operand()
+        M, btype = self._operand(nvec)
         ctl.zero_()
         if consts is None:
             consts = self._const_table()
@@ -262,7 +282,7 @@ class ExpmMultiplyParallel:
         graphs = self.__dict__.setdefault("_graphs", {})
         ent = graphs.get(key)
         if ent is None:
-            _, btype = self._operand()
+            _, btype = self._operand(nvec)
             Fg = F.clone()
             wbuf = torch.empty(2 * n * nvec, dtype=torch.complex64 if btype == _lib.C64 else torch.complex128,
                                device=F.device)

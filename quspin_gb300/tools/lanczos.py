@@ -6,8 +6,10 @@ Drop-in counterparts of QuSpin 1.0.1's ``lanczos_full``, ``lanczos_iter``,
 (scale, product, the two axpys, the dot product and the norm) runs on the
 GPU with alpha/beta kept in device arrays; only the m x m tridiagonal
 eigenproblem is solved on the host (scipy ``eigh_tridiagonal``), as in the
-reference.  ``full_ortho=True`` keeps the reference's post-hoc QR + projection
-(:206-222); ``reorth=True`` is this package's per-step full
+reference.  ``full_ortho=True`` keeps the reference's post-hoc
+orthonormalisation + projection (:206-222), with the orthonormalisation by
+classical Gram-Schmidt twice and the projection as one FP64 tensor-instruction
+block product (csrc/dense.cu); ``reorth=True`` is this package's per-step full
 reorthogonalisation (classical Gram-Schmidt twice against every previous
 Lanczos vector), for long runs where the plain recurrence loses orthogonality.
 """
@@ -171,12 +173,14 @@ def lanczos_full(A, v0, m, full_ortho=False, out=None, eps=None, reorth=False, p
     a, b, m_eff, r, _ = _recurrence(op, Q[0], m, eps, Q=Q, reorth=reorth)
     m = m_eff
     if full_ortho:
-        q, _ = torch.linalg.qr(Q[:m].T)
-        Q[:m] = q.T
-        h = np.zeros((m, m), dtype=np.float64)
+        # orthonormalise Q[:m], then h[i, j] = <A q_i | q_j> (its upper
+        # triangle is what the reference fills, :211-220) as one block
+        # product of the rows R[i] = A q_i with the rows of Q
+        _orthonormalize_rows(Q, m)
+        R = torch.empty_like(Q[:m])
         for i in range(m):
-            op(Q[i], r)
-            h[i, i:] = D.to_host((Q[i:m] @ r.conj()).real)
+            op(Q[i], R[i])
+        h = D.to_host(_block_inner(R, Q[:m], conj=True, xrows=True).real)
         E, V = np.linalg.eigh(h, UPLO="U")
     else:
         E, V = eigh_tridiagonal(a[:m], b[:m - 1])
@@ -316,10 +320,67 @@ def _q_block(Q_T):
 
 
 def _apply_block(A, X):
-    """A X for a device block X [n, k] through the operator's own dot."""
-    if hasattr(A, "dot"):
+    """A X for a device block X [n, k] on the device: the package's operators
+    and device matrices through their own dot, scipy / numpy matrices after
+    conversion to a device CSR.  Anything else must return a CUDA tensor from
+    ``dot`` of a CUDA tensor (no host round trip)."""
+    from ..operators import hamiltonian, quantum_LinearOperator
+    if isinstance(A, (hamiltonian, quantum_LinearOperator, DeviceCSR, DeviceDIA)):
         return A.dot(X)
-    return D.to_device(A @ D.to_host(X))
+    if isinstance(A, np.ndarray) or hasattr(A, "tocsr"):
+        import scipy.sparse as sp
+        return to_device_matrix(sp.csr_matrix(A)).dot(X)
+    if hasattr(A, "dot"):
+        Y = A.dot(X)
+        if D.is_device_array(Y):
+            return Y
+    raise TypeError("operators must be a hamiltonian, quantum_LinearOperator, device or scipy/numpy matrix, "
+                    "or an object whose dot maps CUDA tensors to CUDA tensors")
+
+
+def _block_inner(Q, X, conj=True, xrows=False):
+    """W = op(Q) X on the device (csrc/dense.cu, FP64 tensor-instruction
+    panels): Q [m, n] rows, X [n, k] C order or, with xrows, [k, n] rows;
+    op = complex conjugate when conj.  Real operands stay real."""
+    cplx = Q.is_complex() or X.is_complex()
+    dt = torch.complex128 if cplx else torch.float64
+    Q = Q.to(dt).contiguous()
+    X = X.to(dt).contiguous()
+    m, n = Q.shape
+    k = X.shape[0] if xrows else X.shape[1]
+    W = torch.empty((m, k), dtype=dt, device=D.device())
+    scr = D.scratch_doubles(_lib.load().qs_block_inner_scratch_doubles(n, m, k, int(cplx)))
+    dv = lambda t: D.ptr(torch.view_as_real(t) if t.is_complex() else t)
+    _lib.call("qs_block_inner", n, m, k, dv(Q), n, dv(X), X.shape[1], int(xrows), int(cplx), int(conj), dv(W),
+              D.ptr(scr), D.stream())
+    return W
+
+
+def _orthonormalize_rows(Q, m):
+    """Q[:m] <- orthonormal rows spanning the same nested subspaces: classical
+    Gram-Schmidt applied twice per row against the rows before it, then
+    normalisation, on the device (csrc/lanczos.cu).  This is the QR step of
+    full_ortho (_lanczos_utils.py:206-209); each row keeps the direction of
+    its own component orthogonal to the earlier rows (R has a positive
+    diagonal), where LAPACK's Householder QR may flip the sign of a row."""
+    n = Q.shape[1]
+    cplx = int(Q.is_complex())
+    n2 = n * (2 if cplx else 1)
+    L = _lib.load()
+    st = D.stream()
+    ctl = torch.zeros(2, dtype=torch.int32, device=D.device())
+    ctl[1] = m
+    scr = D.scratch_doubles(L.qs_lanczos_scratch_doubles())
+    rscr = D.scratch_doubles(L.qs_lanczos_reorth_scratch_doubles(m))
+    nrm = torch.zeros(1, dtype=torch.float64, device=D.device())
+    dv = lambda t: D.ptr(torch.view_as_real(t) if t.is_complex() else t)
+    for i in range(m):
+        if i:
+            _lib.check(L.qs_lanczos_reorth(n, cplx, i, dv(Q), n, dv(Q[i]), 2, D.ptr(rscr), D.ptr(ctl), st),
+                       "qs_lanczos_reorth")
+        _lib.check(L.qs_lanczos_beta(n2, dv(Q[i]), None, dv(Q[i]), 0, D.ptr(nrm), 0.0, i, D.ptr(scr), D.ptr(ctl),
+                                     st), "qs_lanczos_beta")
+        _lib.check(L.qs_lanczos_scale(n2, dv(Q[i]), D.ptr(nrm), dv(Q[i]), D.ptr(ctl), st), "qs_lanczos_scale")
 
 
 def FTLM_static_iteration(O_dict, E, V, Q_T, beta=0):
@@ -338,8 +399,7 @@ def FTLM_static_iteration(O_dict, E, V, Q_T, beta=0):
     res = {}
     for key, A in O_dict.items():
         Ar = _apply_block(A, r)
-        Qc = Q.to(torch.promote_types(Q.dtype, Ar.dtype))
-        ov = D.to_host(Qc.conj() @ Ar.to(Qc.dtype))                # <q_a | O q_0>, a = 0..m-1
+        ov = D.to_host(_block_inner(Q, Ar.reshape(-1, 1))[:, 0])   # <q_a | O q_0>, a = 0..m-1
         res[key] = np.squeeze(np.tensordot(ov, c[:ov.shape[0]], axes=(0, 0)))
     return res, np.squeeze(c[0, ...])
 
@@ -370,8 +430,7 @@ def LTLM_static_iteration(O_dict, E, V, Q_T, beta=0):
     res = {}
     for key, A in O_dict.items():
         AX = _apply_block(A, X)                                    # [n, nv]: columns O q_i
-        dt = torch.promote_types(Qn.dtype, AX.dtype)
-        Ome = D.to_host((Qn.to(dt).conj() @ AX.to(dt)).transpose(0, 1))   # [i, j] = <q_j | O q_i>
+        Ome = D.to_host(_block_inner(Qn, AX).transpose(0, 1))     # [i, j] = <q_j | O q_i>
         A_diag = Vn.T.dot(Ome.dot(Vn))
         res[key] = np.squeeze(np.einsum("j...,l...,jl->...", cc, cc, A_diag))
     p = np.exp(-np.outer(E[:nv], beta))

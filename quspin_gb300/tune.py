@@ -41,6 +41,18 @@ def occ_candidates(M, nvec, btype):
     return [(G, U) for G in (2, 4) for U in (1, 2)]
 
 
+def r32_candidates(M, nvec, btype):
+    """Shapes of the 32-row single-vector Taylor term (csrc/expm_st.cu; bits
+    20-21 of the launch code: 4, 2 or 8 lanes per row in the gather loop,
+    bits 18-19: 0 / 1 for 4 / 6 resident blocks per SM): one vector, float
+    forms, int32 indices."""
+    if nvec != 1 or btype == _lib.C128 or getattr(M, "idx64", 0):
+        return []
+    if M.vcode not in (_lib.PF8, _lib.CPF8, _lib.PF8P, _lib.CPF8P, _lib.PF, _lib.CPF, _lib.F32, _lib.C64):
+        return []
+    return [(shape, occ) for shape in (1, 2, 3) for occ in (0, 1)]
+
+
 def _time(fn, reps=5):
     st = torch.cuda.current_stream()
     for _ in range(2):
@@ -91,7 +103,7 @@ def tune_taylor(M, nvec, btype):
     b0 = torch.ones(n * nvec, dtype=bdt, device=D.device())
     b1 = torch.empty_like(b0)
     F = torch.zeros(n * nvec, dtype=torch.complex128, device=D.device())
-    ctl = torch.zeros(6, dtype=torch.int64, device=D.device())
+    ctl = torch.zeros(max(_lib.load().qs_expm_ctl_bytes() // 8, 1) + 1, dtype=torch.int64, device=D.device())
     coeff = torch.tensor([1e-3 + 0j], dtype=torch.complex128, device=D.device())
     best, best_t = 0, None
     cands = [(G, U, 0) for G, U in _candidates(n, M.nnz, nvec)]
@@ -100,8 +112,11 @@ def tune_taylor(M, nvec, btype):
         # chunk-outer sweeps of 4 vectors keep a narrower slice of B in L2
         # (8-vector sweeps never beat the one-sweep order in measurements)
         cands += [(G, U, 3) for G, U, _ in cands]
-        rown = torch.empty(2 * n, dtype=torch.float32, device=D.device())
+        rown = torch.empty(2 * n, dtype=torch.float64, device=D.device())
     cands += [(G, U, occ << 2) for G, U in occ_candidates(M, nvec, btype) for occ in (1, 2)]
+    if getattr(M, "vcode", None) in (_lib.PF8P, _lib.CPF8P):
+        cands = []                 # the packed form runs only in the 32-row kernel
+    cands += [({1: 4, 2: 2, 3: 8}[shape], 2, (shape << 4) | (occ << 2)) for shape, occ in r32_candidates(M, nvec, btype)]
     for G, U, ch in cands:
         code = encode(G, U) | (ch << 16)
 
@@ -113,4 +128,5 @@ def tune_taylor(M, nvec, btype):
         if best_t is None or t < best_t:
             best, best_t = code, t
     cache[key] = best
+    M.__dict__.setdefault("_tuned_ms", {})[key] = best_t
     return best

@@ -1,5 +1,5 @@
-"""Generates tests/golden/*.npz (run once in a container that has the
-reference checkout at /root/reference; the fixtures are committed).
+"""Generates tests/golden/*.npz (run once where a checkout of the reference
+project is available; the fixtures are committed).
 
 What runs from the reference itself:
   * src/quspin/tools/lanczos/_lanczos_utils.py and _expm.py, imported
@@ -15,7 +15,9 @@ What runs from the reference itself:
 The basis and Hamiltonian come from the oracle restatement (the reference's
 native basis core is not installable here).
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
+        (or set QUSPIN_REFERENCE_ROOT; REFERENCE_ROOT is the directory that
+        holds the reference's src/, docs/ and test/ folders)
 """
 import html
 import importlib.util
@@ -30,7 +32,7 @@ from scipy.sparse.linalg import expm_multiply
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QUSPIN_REFERENCE_ROOT", "")
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
@@ -130,6 +132,8 @@ def thermal_fixture(lz):
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "src", "quspin")):
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set QUSPIN_REFERENCE_ROOT)")
     L = 20
     m = chain_maps(L)
     blocks = dict(kblock=(m["t"], 0), pblock=(m["p"], 0))

@@ -34,7 +34,7 @@ def test_binding_matches_header():
     L = _lib()
     assert set(L.exported_names()) == _declared()
     lib = L.load()
-    assert lib.qs_expm_ctl_bytes() == 48
+    assert lib.qs_expm_ctl_bytes() == 56
     assert lib.qs_enum_num_candidates(32, 1, 16, 0) == 601080390
     assert lib.qs_enum_num_candidates(32, 2, 5, 5) == 4368 * 4368
     assert lib.qs_scan_scratch_elems(10) >= 1

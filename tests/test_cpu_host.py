@@ -49,3 +49,81 @@ def test_launch_code_layout():
     assert occ_candidates(M, 1, _lib.C128) == []
     M64 = type("M", (), {"idx64": 1})()
     assert occ_candidates(M64, 1, _lib.CPF) == []
+
+
+def _powers_by_steps(map):
+    """The reference's definition of the period (base_general.py:22-51),
+    stepped one application at a time: labels move to map[i], an inverted
+    site turns label x into -(x + 1); stop when the identity comes back."""
+    m = np.asarray(map)
+    dest = np.where(m < 0, -m - 1, m)
+    sites = np.arange(len(m))
+    start = sites.copy()
+    seen = [tuple(sites)]
+    while True:
+        sites = np.where(m < 0, -sites - 1, sites)[dest]
+        seen.append(tuple(int(x) for x in sites))
+        if np.array_equal(sites, start):
+            return len(seen) - 1, set(seen)
+
+
+def test_process_map_period_and_group_match_stepwise_definition():
+    import warnings
+    from oracle import oracle as O
+    from quspin_gb300.basis import GeneralBasisWarning, process_map
+    rng = np.random.default_rng(3)
+    L = 12
+    s = np.arange(L)
+    maps = [(s + 1) % L, s[::-1].copy(), -(s + 1), -(((s + 1) % L) + 1), np.where(s % 3 == 0, -(s[::-1] + 1), s[::-1])]
+    for _ in range(40):
+        perm = rng.permutation(L)
+        flip = rng.random(L) < 0.3
+        maps.append(np.where(flip, -(perm + 1), perm))
+    for m in maps:
+        out_map, per, q, group = process_map(m, 3)
+        per_ref, group_ref = _powers_by_steps(m)
+        assert per == per_ref == O.process_map(m, 3)[1]
+        assert group == group_ref and q == 3 and out_map.dtype == np.int32
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        assert process_map(s, 0)[1] == 1
+        assert any(issubclass(x.category, GeneralBasisWarning) for x in w)
+    try:
+        process_map(np.array([0, 0, 2]), 0)
+    except ValueError as e:
+        assert str(e) == "map must be a one-to-one site mapping."
+    else:
+        raise AssertionError("expected ValueError")
+
+
+def test_consolidate_static_merges_bonds_and_drops_tiny_couplings():
+    """_make_hamiltonian._consolidate_static (:19-41): repeated (opstr, sites)
+    bonds are summed, couplings with |J| <= 10 eps are dropped."""
+    from oracle import oracle as O
+    from quspin_gb300.operators import _consolidate_static
+    eps = np.finfo(np.float64).eps
+    static = [["zz", [[1.0, 0, 1], [0.5, 1, 2], [0.25, 0, 1]]],
+              ["+-", [[0.5, 0, 1], [5 * eps, 2, 3], [0.5, 1, 2]]],
+              ["zz", [[-0.5, 1, 2], [2.0, 2, 3]]],
+              ["x", [[1e-3, 0], [-1e-3, 0]]]]
+    out = _consolidate_static(static)
+    assert out == O.consolidate_static(static)
+    d = {(o, tuple(ix)): J for o, ix, J in out}
+    assert d[("zz", (0, 1))] == 1.25
+    assert ("zz", (1, 2)) not in d                 # 0.5 - 0.5 = 0 dropped
+    assert d[("zz", (2, 3))] == 2.0
+    assert ("+-", (2, 3)) not in d                 # 5 eps <= 10 eps dropped
+    assert ("x", (0,)) not in d                    # exact cancellation
+    assert len(out) == 4
+
+
+def test_r32_candidates_need_one_vector_float_forms():
+    from quspin_gb300.tune import r32_candidates
+
+    def M(vcode, idx64=0):
+        return type("M", (), {"idx64": idx64, "vcode": vcode})()
+    assert r32_candidates(M(_lib.PF8P), 1, _lib.CPF) == [(s, o) for s in (1, 2, 3) for o in (0, 1)]
+    assert len(r32_candidates(M(_lib.PF8), 1, _lib.CPF)) == 6
+    assert r32_candidates(M(_lib.PF8), 2, _lib.CPF) == []
+    assert r32_candidates(M(_lib.PF8), 1, _lib.C128) == []
+    assert r32_candidates(M(_lib.PF8, idx64=1), 1, _lib.CPF) == []

@@ -144,7 +144,7 @@ def test_chunk_outer_sweep_matches_row_order(cuda):
         res = []
         for chunk in (0, 1):
             op = ExpmMultiplyParallel(DeviceCSR.from_scipy(A), a=-0.5j, precision=prec)
-            M, _ = op._operand()
+            M, _ = op._operand(16)
             M.__dict__.setdefault("_tuned", {})[("taylor", 16, bt)] = encode(4, 1) | (chunk << 16)
             F = torch.tensor(V, device="cuda")
             op.run_device(F)

@@ -1,0 +1,108 @@
+"""The 32-row single-vector Taylor term (csrc/expm_st.cu) against the
+row-handout term (csrc/expm_lp.cu) on the same inputs: one term gives
+bit-identical B, F and stopping-test norm for every value form (coded,
+coded with the codes packed into the column words, one pair per nonzero,
+complex coded, and the complex64 form) and every lane count, on a matrix
+with an odd number of rows, empty rows and one long row; whole evolutions
+through ExpmMultiplyParallel are bit-identical too."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _matrix(n=70001, complex_vals=False, seed=0):
+    rng = np.random.default_rng(seed)
+    nnz = 24 * n
+    r, c = rng.integers(0, n, nnz), rng.integers(0, n, nnz)
+    vals = rng.choice(np.array([0.5, -0.5, 0.25, 1.0, -1.5, 0.7071067811865476]), nnz)
+    if complex_vals:
+        vals = vals * np.exp(1j * rng.choice(np.array([0.0, 0.5, 1.0]), nnz))
+    A = sp.csr_matrix((vals, (r, c)), shape=(n, n))
+    A = sp.csr_matrix(A + A.conj().T)
+    A = A.tolil()
+    A[n // 3, :] = 0                                       # an empty row
+    A[n // 2, np.arange(0, n, 37)] = 0.5                   # a long row
+    A = sp.csr_matrix(A)
+    A.sum_duplicates()
+    return A
+
+
+def _term(M, code, B_in, F_in, btype):
+    from quspin_gb300 import _device as D
+    from quspin_gb300 import _lib
+    n = M.shape[0]
+    F = F_in.clone()
+    Bout = torch.zeros_like(B_in)
+    ctl = torch.zeros(_lib.load().qs_expm_ctl_bytes() // 8 + 1, dtype=torch.int64, device="cuda")
+    coeff = torch.tensor([0.03 - 0.02j], dtype=torch.complex128, device="cuda")
+    _lib.call("qs_taylor_term", n, M.nnz, D.ptr(M.indptr), M.idx64, D.ptr(M.indices), D.ptr(M.data), M.vcode,
+              D.ptr(B_in), D.ptr(Bout), btype, D.ptr(F), 1, 0.37, 0.0, D.ptr(coeff), 0, 0.0, D.ptr(ctl), code,
+              D.stream())
+    torch.cuda.synchronize()
+    assert int(ctl.view(torch.int32)[12].item()) == 0
+    return Bout, F, float(ctl.view(torch.float64)[0].item())
+
+
+def _same(a, b):
+    return torch.equal(a.view(torch.int64) if a.dtype == torch.complex128 else a.view(torch.int32),
+                       b.view(torch.int64) if b.dtype == torch.complex128 else b.view(torch.int32))
+
+
+@pytest.mark.parametrize("complex_vals", [False, True])
+def test_r32_term_bitwise_equal_to_row_handout(cuda, complex_vals):
+    from quspin_gb300 import _device as D
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tune import encode
+    A = _matrix(complex_vals=complex_vals)
+    Ad = DeviceCSR.from_scipy(A)
+    n = A.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(1)
+    v = torch.randn(n, dtype=torch.complex128, generator=g).to("cuda")
+    F0 = torch.randn(n, dtype=torch.complex128, generator=g).to("cuda")
+    Bp = torch.empty(n, dtype=torch.complex128, device="cuda")          # float-pair storage, 16 bytes per element
+    _lib.call("qs_split_pairs", 2 * n, D.ptr(v), D.ptr(Bp), D.stream())
+    coded = Ad.paired(coded=True)
+    assert coded.coded
+    forms = [coded, coded.packed(), Ad.paired(coded=False)]
+    for G, shape in ((4, 1), (2, 2), (8, 3)):
+        ref = _term(coded, encode(G, 2), Bp, F0, _lib.CPF)
+        for M in forms:
+            for occ in (0, 1):
+                out = _term(M, encode(G, 2) | (occ << 18) | (shape << 20), Bp, F0, _lib.CPF)
+                assert _same(out[0], ref[0]) and _same(out[1], ref[1]), (G, M.vcode, occ)
+                assert out[2] == ref[2]
+    # complex64 form: float32 / complex64 values, complex64 B
+    M32 = Ad.astype(np.complex64 if complex_vals else np.float32)
+    B32 = v.to(torch.complex64)
+    for G, shape in ((4, 1), (2, 2)):
+        ref = _term(M32, encode(G, 2), B32, F0, _lib.C64)
+        out = _term(M32, encode(G, 2) | (shape << 20), B32, F0, _lib.C64)
+        assert _same(out[0], ref[0]) and _same(out[1], ref[1]) and out[2] == ref[2]
+
+
+def test_r32_evolution_bitwise_equal(cuda):
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    from quspin_gb300.tune import encode
+    A = _matrix(seed=3)
+    n = A.shape[0]
+    rng = np.random.default_rng(4)
+    v = rng.normal(size=n) + 1j * rng.normal(size=n)
+    v /= np.linalg.norm(v)
+    out = []
+    for packed, code in ((False, encode(4, 2)), (False, encode(4, 2) | (1 << 20)), (True, encode(4, 2) | (1 << 20))):
+        op = ExpmMultiplyParallel(DeviceCSR.from_scipy(A), a=-0.8j)
+        P = op.A_device.paired()
+        M = P.packed() if packed else P
+        op._pick = M
+        M.__dict__.setdefault("_tuned", {})[("taylor", 1, _lib.CPF)] = code
+        F = torch.tensor(v, device="cuda")
+        op.run_device(F)
+        out.append(F.cpu().numpy())
+    assert np.array_equal(out[0].view(np.int64), out[1].view(np.int64))
+    assert np.array_equal(out[0].view(np.int64), out[2].view(np.int64))

@@ -51,13 +51,22 @@ def test_expm_noalloc_matches_allocating_entry_point(cuda):
                             D.ptr(consts[k:k + 1]), D.ptr(consts[k + 1:]), D.ptr(work), _lib.C128, D.ptr(ctl), 0,
                             D.stream())
     assert rc == 0
-    for _ in range(2):
-        F = v.clone()
+    outs = [v.clone() for _ in range(2)]
+    torch.cuda.synchronize()
+    free_after_setup = None
+    for i, F in enumerate(outs):
         rc = L.qs_expm_multiply_noalloc(n, A.nnz, D.ptr(A.indptr), A.idx64, D.ptr(A.indices), D.ptr(A.data),
                                         D.code(A.dtype), D.ptr(F), nvec, s, m, tol, mu.real, mu.imag, a.real, a.imag,
                                         0, D.stream())
         assert rc == 0
         torch.cuda.synchronize()
+        if i == 0:
+            # after the first (set-up) call on this device
+            free_after_setup = torch.cuda.mem_get_info()[0]
+        else:
+            # the second call allocated no device memory (cudaMemGetInfo unchanged)
+            assert torch.cuda.mem_get_info()[0] == free_after_setup
+    for F in outs:
         err = (torch.linalg.vector_norm(F - F_ref) / torch.linalg.vector_norm(F_ref)).item()
         assert err <= 1e-12, err
     # sizes beyond the static scratch are rejected before any work
