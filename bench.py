@@ -74,19 +74,46 @@ def peak_hbm():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profile_traffic():
-    """dram bytes per launch of the Taylor-term kernel from the committed ncu
-    summary (a 'traffic_bytes_per_launch_full: <int>' line), else None."""
+KERNEL_SOURCES = {
+    "taylor_r32_kernel": ["expm_st.cu", "lp_modes.cuh", "pairf.cuh", "expm_ctl.cuh", "qs_common.cuh"],
+    "taylor_rows_kernel": ["expm_st.cu", "lp_modes.cuh", "pairf.cuh", "expm_ctl.cuh", "qs_common.cuh"],
+    "taylor_lp_kernel": ["expm_lp.cu", "lp_modes.cuh", "pairf.cuh", "expm_ctl.cuh", "qs_common.cuh"],
+}
+
+
+def kernel_source_sha(kernel):
+    """sha256 over the CUDA sources a kernel is compiled from."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES.get(kernel, []):
+        with open(os.path.join(ROOT, "quspin_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch of the Taylor-term kernel from the committed ncu
+    summary of the same kernel at this workload, as (bytes, note).  The
+    summary records the kernel's name and the sha256 of its sources at
+    capture time ('traffic_kernel:', 'traffic_source_sha256:',
+    'traffic_bytes_per_launch_full:' lines); a capture of another kernel or of
+    other sources gives (None, reason) instead of a stale number."""
     p = os.path.join(ROOT, "profiles", "taylor_term_j1j2.md")
     if not os.path.exists(p):
-        return None
+        return None, "no ncu summary"
+    rec = {}
     for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch_full:"):
-            try:
-                return float(line.split(":", 1)[1].strip())
-            except ValueError:
-                return None
-    return None
+        for key in ("traffic_kernel", "traffic_source_sha256", "traffic_bytes_per_launch_full"):
+            if line.strip().startswith(key + ":"):
+                rec[key] = line.split(":", 1)[1].strip()
+    if rec.get("traffic_kernel") != kernel:
+        return None, "the ncu summary covers {}, not {}".format(rec.get("traffic_kernel"), kernel)
+    if rec.get("traffic_source_sha256") != kernel_source_sha(kernel):
+        return None, "the kernel's sources changed since the ncu capture"
+    try:
+        return float(rec["traffic_bytes_per_launch_full"]), "ncu capture (profiles/taylor_term_j1j2.md), same sources"
+    except (KeyError, ValueError):
+        return None, "no traffic line in the ncu summary"
 
 
 class ClockSampler:
@@ -181,7 +208,8 @@ def build_problem(L, J1, J2):
 
 def taylor_kernel_name(group):
     """Kernel the launch code selects for one vector in the float forms."""
-    return "taylor_r32_kernel" if (group >> 20) & 3 else "taylor_lp_kernel"
+    shape = (group >> 20) & 7
+    return "taylor_rows_kernel" if shape >= 4 else ("taylor_r32_kernel" if shape else "taylor_lp_kernel")
 
 
 def taylor_term_bytes(n, nnz, nvec=1, vb=8):
@@ -485,6 +513,62 @@ def cpu_baseline(A, v, op, budget_s=12.0):
             "seconds_per_term": T / max(sum(ev.terms), 1)}
 
 
+def learned_partition_ablation(A, v_dev, op_plain, t_setup_plain, t_evo_plain, F_plain):
+    """The benchmark operator with the (m*, s) selection from the learned
+    norm-ratio predictor instead of onenormest: predictor trained here on the
+    GPU on J1-J2 chains L = 16 .. 26 (J2 = 0.25, 0.5, 0.75, both z sectors);
+    set-up time, (m*, s), Taylor terms, evolution time and state error
+    against the plain selection's state."""
+    import torch
+    from quspin_gb300 import hamiltonian, spin_basis_general
+    from quspin_gb300.learned import NormRatioPredictor, norm_ratio_training_set
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    W = WORKLOAD
+    t0 = time.perf_counter()
+    mats = []
+    for L in (16, 18, 20, 22, 24, 26):
+        s_ = np.arange(L)
+        for z in (0, 1):
+            b = spin_basis_general(L, Nup=L // 2, pauli=0, kblock=((s_ + 1) % L, 0), pblock=(s_[::-1].copy(), 0),
+                                   zblock=(-(s_ + 1), z))
+            for J2 in (0.25, 0.5, 0.75):
+                mats.append(hamiltonian(j1j2_static(L, 1.0, J2), [], basis=b, dtype=np.float64).tocsr_gpu())
+    f, r = norm_ratio_training_set(mats)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pred = NormRatioPredictor(seed=0)
+    hist = pred.fit(f, r, epochs=600)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    op = ExpmMultiplyParallel(A, a=-1j * W["t"], predictor=pred)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    F = v_dev.clone()
+    op.run_device(F)
+    torch.cuda.synchronize()
+    reps = 3
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        F.copy_(v_dev)
+        op.run_device(F)
+    e1.record(st)
+    torch.cuda.synchronize()
+    t_evo = e0.elapsed_time(e1) / 1e3 / reps
+    err = float(torch.linalg.vector_norm(F - F_plain) / torch.linalg.vector_norm(F_plain))
+    side = lambda o, ts, te: {"setup_s": round(ts, 4), "m_star": int(o.m_star), "s": int(o.s),
+                              "norm_products": int(o.norm_products), "terms_per_evolution": int(o.terms_executed),
+                              "evolution_s": round(te, 5), "evolutions_per_s_with_setup": 1.0 / (ts + te)}
+    return {"training": {"operators": len(mats), "labels_s": round(t_data, 2), "train_s": round(t_train, 2),
+                         "loss_first_last": [hist[0], hist[-1]]},
+            "plain": side(op_plain, t_setup_plain, t_evo_plain),
+            "learned": dict(side(op, t_setup, t_evo), partition_source=op.partition_source, fallbacks=op.fallbacks),
+            "rel_state_error_vs_plain": err,
+            "setup_speedup": t_setup_plain / max(t_setup, 1e-9)}
+
+
 def run_ours(args, rank, ws):
     import torch
     from quspin_gb300.tools import ExpmMultiplyParallel
@@ -562,6 +646,7 @@ def run_ours(args, rank, ws):
     t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8 = time_kernels(op, v_dev)
     lib_ctx = library_spmv(A, v_dev, spmv_bytes(n, nnz)) if A.dtype == np.float64 else {"unavailable": "complex"}
     peak, peak_kind = peak_hbm()
+    traffic, traffic_note = profile_traffic(taylor_kernel_name(group))
     P, _ = op._operand(1)           # the operand form the evolution runs on (coded, or codes packed in the indices)
     vb = P.value_bytes
     probe = gather_probe(A, v_dev)
@@ -586,10 +671,10 @@ def run_ours(args, rank, ws):
         "e2e": {"value": ws * args.steps / T_e2e, "unit": "evolutions/s", "h2d_bytes_per_step": int(n * 16),
                 "d2h_bytes_per_step": int(n * 16)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": profile_traffic(), "kernel": taylor_kernel_name(group),
+                     "peak_source": peak_kind, "traffic": traffic, "traffic_source": traffic_note, "kernel": taylor_kernel_name(group),
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
                      "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff,
-                                      "blocks_per_sm_cap": ({0: 4, 1: 6} if (group >> 20) & 3 else
+                                      "blocks_per_sm_cap": ({0: 4, 1: 6} if (group >> 20) & 7 else
                                                             {0: None, 1: 6, 2: 8}).get((group >> 18) & 3)},
                      "operand": "codes packed in the column words" if vb == 0 else "coded values",
                      "value_bytes_per_nonzero": vb, "distinct_values": getattr(P, "distinct", None),
@@ -605,6 +690,14 @@ def run_ours(args, rank, ws):
         "clocks": clk.summary(),
         "state_norm_error": norm_err,
     }
+    if rank == 0 and not args.no_learned:
+        F_plain = v_dev.clone()
+        op.run_device(F_plain)
+        torch.cuda.synchronize()
+        try:
+            out["learned_partition"] = learned_partition_ablation(A, v_dev, op, t_setup, T / args.steps, F_plain)
+        except Exception as e:  # report, never fake
+            out["learned_partition"] = {"error": str(e)[:300]}
     if rank == 0 and ws == 1 and not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline(A.tocsr(), v_host, op)
@@ -1103,6 +1196,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-partition ablation")
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
     p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
     p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard", "lanczos",

@@ -294,10 +294,11 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // per lane; C = 1 asks the float forms for the chunk-outer sweep, which takes
 // effect only through qs_taylor_term_rows with a row-sum scratch; bit 17
 // narrows its chunks from 8 to 4 vectors; bits 18-19 cap the registers of the
-// single-vector float-pair shapes for 6 / 8 blocks per SM; bits 20-21 = 1..3
-// select the staged single-vector kernel of csrc/expm_st.cu with unit shape
-// 1: 4 lanes x 8 rows, 2: 4 lanes x 16 rows, 3: 2 lanes x 16 rows -- one
-// vector, int32 indices, 16-byte aligned index and value arrays);
+// single-vector float-pair shapes for 6 / 8 blocks per SM; bits 20-22 = 1..5
+// select a single-vector kernel of csrc/expm_st.cu: 1..3 the 32-row kernel
+// with 4, 2 or 8 lanes per row, 4..5 the persistent row-handout kernel with
+// 2 or 4 lanes per row (bit 18 then caps registers for 6 blocks per SM) --
+// one vector, int32 indices; the packed value forms 8 / 9 run only there);
 // 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                                    const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
@@ -338,7 +339,7 @@ extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, i
                  ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
         a.occ = group > 0 ? (group >> 18) & 3 : 0;
         a.nnz = nnz;
-        a.staged = group > 0 ? (group >> 20) & 3 : 0;
+        a.staged = group > 0 ? (group >> 20) & 7 : 0;
         if (a.staged) return st_taylor_term(a);
         return lp_taylor_term(a, false);
     }

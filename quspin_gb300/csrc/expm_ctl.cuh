@@ -125,10 +125,10 @@ struct LpTerm {
     cudaStream_t st;
     int occ = 0;              // single-vector float-pair shapes: 1 / 2 cap registers for 6 / 8 blocks per SM
     int64_t nnz = 0;          // stored entries (the staged kernel's copy bounds)
-    int staged = 0;           // 1..3: staged single-vector kernel (csrc/expm_st.cu) with unit shape 1..3
+    int staged = 0;           // 1..5: single-vector kernel of csrc/expm_st.cu (1..3 32-row, 4..5 row hand-out)
 };
 
-// The staged single-vector term (csrc/expm_st.cu).
+// The single-vector terms of csrc/expm_st.cu.
 int st_taylor_term(const LpTerm &a);
 
 int lp_taylor_term(const LpTerm &a, bool multi);

@@ -231,8 +231,8 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                     atomicMax(&s_mf[sec], (unsigned long long)__double_as_longlong(rfn));
                 }
             } else {
-                mb = fmaxf(mb, rbn);
-                mf = fmaxf(mf, rfn);
+                mb = fmax(mb, rbn);
+                mf = fmax(mf, rfn);
             }
         }
     }
@@ -442,12 +442,16 @@ int lp_go(const LpTerm &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
-    const int blocks = taylor_grid(a.n, a.G);
+    // persistent grid: the kernels stride over row groups, so one wave of
+    // resident blocks does all rows without per-block set-up repeated
+    const int64_t need = taylor_grid(a.n, a.G);
+    static int resident[4] = {0, 0, 0, 0};
     double2 *rn = a.chunk_outer ? (double2 *)a.rownorm : nullptr;
     if constexpr (NB == 1 && U <= 2 && sizeof(IT) == 4 && std::is_same<M, ModePF>::value) {
         if (a.occ == 1 || a.occ == 2) {
             auto k = a.occ == 1 ? taylor_lp_kernel_occ6<M, DV, IT, NB, U, MULTI, CODED>
                                 : taylor_lp_kernel_occ8<M, DV, IT, NB, U, MULTI, CODED>;
+            const int blocks = qs_persistent_grid(k, 256, need, resident[a.occ]);
             k<<<blocks, 256, 0, a.st>>>(a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data,
                                         (const typename M::BE *)a.Bin, (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0,
                                         a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
@@ -455,14 +459,19 @@ int lp_go(const LpTerm &a)
             return QS_OK;
         }
     }
-    if constexpr (NB >= 8)
-        taylor_lp_kernel_wide<M, DV, IT, NB, U, MULTI, CODED><<<blocks, 256, 0, a.st>>>(
-            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
-    else
-        taylor_lp_kernel<M, DV, IT, NB, U, MULTI, CODED><<<blocks, 256, 0, a.st>>>(
-            a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, (const typename M::BE *)a.Bin,
-            (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0, a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
+    if constexpr (NB >= 8) {
+        auto k = taylor_lp_kernel_wide<M, DV, IT, NB, U, MULTI, CODED>;
+        const int blocks = qs_persistent_grid(k, 256, need, resident[3]);
+        k<<<blocks, 256, 0, a.st>>>(a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data,
+                                    (const typename M::BE *)a.Bin, (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0,
+                                    a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
+    } else {
+        auto k = taylor_lp_kernel<M, DV, IT, NB, U, MULTI, CODED>;
+        const int blocks = qs_persistent_grid(k, 256, need, resident[0]);
+        k<<<blocks, 256, 0, a.st>>>(a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data,
+                                    (const typename M::BE *)a.Bin, (typename M::BE *)a.Bout, a.F, a.nvec, a.mu0,
+                                    a.mus, a.sec_off, a.coeff, a.j, a.tol, a.ctl, rn);
+    }
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }

@@ -1,4 +1,5 @@
-// Single-vector fused Taylor term with a 32-row epilogue.
+// Single-vector fused Taylor terms: a 32-row epilogue kernel and a
+// persistent row-handout kernel.
 //
 // The same term as csrc/expm_lp.cu (new B = cf (A - mu) B, F += new B, both
 // infinity norms and the stopping test of scipy's _expm_multiply_simple_core,
@@ -181,6 +182,131 @@ __device__ __forceinline__ void r32_body(int64_t n, const int32_t *__restrict__ 
     }
 }
 
+// Row hand-out (G lanes per row, 32/G rows per warp at a time, the row
+// epilogue right after each row's gathers) as in csrc/expm_lp.cu, specialised
+// for one vector and one matrix, with a persistent grid and the packed value
+// form.  Measured on the L=32 J1-J2 sector this shape at G = 2 is the
+// fastest single-vector term: with two lanes per row both lanes of a group
+// write (one component each), so no epilogue lane idles.
+template <class M, class DV, int VMODE, int G, int U>
+__device__ __forceinline__ void rows_body(int64_t n, const int32_t *__restrict__ indptr,
+                                          const int32_t *__restrict__ indices, const DV *__restrict__ data,
+                                          const typename M::BE *__restrict__ Bin, typename M::BE *__restrict__ Bout,
+                                          cdbl *__restrict__ F, cdbl mu0, const cdbl *__restrict__ coeff, int j,
+                                          double tol, ExpmCtl *ctl)
+{
+    using S = typename M::S;
+    using BE = typename M::BE;
+    constexpr bool CODED = VMODE != 0;
+    constexpr int GPW = 32 / G;
+    __shared__ S s_c[4];
+    __shared__ int s_bexp;
+    __shared__ DV s_tab[CODED ? QS_CODE_TABLE : 1];
+    if (*((volatile int *)&ctl->done)) return;
+    if (threadIdx.x == 0) s_bexp = *((volatile int *)&ctl->bexp);
+    if (threadIdx.x == 1) {
+        const cx<S> c{M::from_d(coeff[j].x), M::from_d(coeff[j].y)};
+        const cx<S> m{M::from_d(mu0.x), M::from_d(mu0.y)};
+        s_c[2] = M::sub(M::mul(c.re, m.re), M::mul(c.im, m.im));
+        s_c[3] = M::add(M::mul(c.re, m.im), M::mul(c.im, m.re));
+    }
+    if (threadIdx.x == 32) s_c[0] = M::from_d(coeff[j].x);
+    if (threadIdx.x == 33) s_c[1] = M::from_d(coeff[j].y);
+    const uint8_t *codes = nullptr;
+    if constexpr (CODED) {
+        for (int i = threadIdx.x; i < QS_CODE_TABLE; i += blockDim.x) s_tab[i] = ldv(data + i);
+        codes = reinterpret_cast<const uint8_t *>(data + QS_CODE_TABLE);
+    }
+    __syncthreads();
+    const unsigned long long keep = l2_keep_policy();
+    const int bexp = s_bexp;
+    const double s_inv = pow2(-bexp);
+    const int lane = threadIdx.x & (G - 1);
+    const int comp = lane & 1;
+    const int gsub = (threadIdx.x & 31) / G;
+    const S cf_re = s_c[0], cm_re = s_c[2];
+    const S cf_x = comp ? s_c[1] : M::neg(s_c[1]);
+    const S cm_x = comp ? s_c[3] : M::neg(s_c[3]);
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double mb = 0.0, mf = 0.0;
+    for (int64_t rb = warp * GPW; rb < n; rb += nwarps * GPW) {
+        const int64_t r = rb + gsub;
+        const bool valid = r < n;
+        const bool writer = valid && lane < 2;
+        const int32_t k0 = valid ? __ldg(indptr + r) : 0, k1 = valid ? __ldg(indptr + r + 1) : 0;
+        BE bo{M::zero(), M::zero()};
+        double fv = 0.0;
+        if (writer) {
+            bo = M::ldB(Bin + r);
+            fv = __ldcs(reinterpret_cast<const double *>(F + r) + comp);
+        }
+        S ar = M::zero(), ai = M::zero();
+        for (int32_t k = k0 + lane; k < k1; k += G * U) {
+            int32_t col[U];
+            DV d[U];
+#pragma unroll
+            for (int uu = 0; uu < U; uu++) {
+                const int32_t kk = k + uu * G;
+                const bool in = kk < k1;
+                if constexpr (VMODE == 2) {
+                    const uint32_t w = in ? (uint32_t)__ldcs(indices + kk) : 0u;
+                    col[uu] = (int32_t)(w >> 8);
+                    d[uu] = in ? s_tab[w & 255u] : vzero<DV>();
+                } else {
+                    col[uu] = in ? __ldcs(indices + kk) : 0;
+                    if constexpr (VMODE == 1) d[uu] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
+                    else d[uu] = in ? ldv(data + kk) : vzero<DV>();
+                }
+            }
+#pragma unroll
+            for (int uu = 0; uu < U; uu++)
+                if (k + uu * G < k1) vmul_acc<M>(ar, ai, d[uu], M::ldB(Bin + col[uu], keep));
+        }
+#pragma unroll
+        for (int o = G >> 1; o > 0; o >>= 1) {
+            ar = M::merge(ar, M::shfl_xor(ar, o));
+            ai = M::merge(ai, M::shfl_xor(ai, o));
+        }
+        // new term = cf (A B) - (cf mu) B, this lane's component (as csrc/expm_lp.cu)
+        const S acc_c = M::fin(comp ? ai : ar), acc_o = M::fin(comp ? ar : ai);
+        const S bo_c = comp ? bo.im : bo.re, bo_o = comp ? bo.re : bo.im;
+        const S mine = M::sub(M::add(M::mul(cf_re, acc_c), M::mul(cf_x, acc_o)),
+                              M::add(M::mul(cm_re, bo_c), M::mul(cm_x, bo_o)));
+        double md = 0.0, fs = 0.0;
+        if (writer) {
+            M::st_comp(Bout + r, comp, mine);
+            fv = M::add_to(fv, mine, bexp);
+            __stcs(reinterpret_cast<double *>(F + r) + comp, fv);
+            md = M::to_d(mine, 0);
+            fs = fv * s_inv;
+        }
+        double nb2 = __dmul_rn(md, md), f2 = __dmul_rn(fs, fs);
+        nb2 = __dadd_rn(nb2, __shfl_xor_sync(FULL, nb2, 1));
+        f2 = __dadd_rn(f2, __shfl_xor_sync(FULL, f2, 1));
+        if (writer) {
+            mb = fmax(mb, nb2);
+            mf = fmax(mf, f2);
+        }
+    }
+    fold_max2(mb, mf, &ctl->c2, &ctl->fn);
+    if (last_block(ctl) && threadIdx.x == 0) {
+        volatile ExpmCtl *vc = ctl;
+        double c2 = sqrt(__longlong_as_double((long long)vc->c2));
+        double fn = sqrt(__longlong_as_double((long long)vc->fn));
+        const double sc = pow2(s_bexp);
+        c2 *= sc;
+        fn *= sc;
+        vc->terms = vc->terms + 1;
+        if (vc->c1 + c2 <= tol * fn) vc->done = 1;
+        else vc->c1 = c2;
+        vc->c2 = 0ull;
+        vc->fn = 0ull;
+        __threadfence();
+        vc->arrive = 0u;
+    }
+}
+
 #define R32_PARAMS                                                                                             \
     int64_t n, const int32_t *__restrict__ indptr, const int32_t *__restrict__ indices, const DV *__restrict__ data, \
         const typename M::BE *__restrict__ Bin, typename M::BE *__restrict__ Bout, cdbl *__restrict__ F, cdbl mu0,  \
@@ -200,6 +326,17 @@ __global__ void __launch_bounds__(256, 6) taylor_r32_kernel_occ6(R32_PARAMS)
 
 // persistent grid: every resident block, but no more blocks than 8-warp
 // groups of 32-row units
+template <class M, class DV, int VMODE, int G, int U>
+__global__ void __launch_bounds__(256, 4) taylor_rows_kernel(R32_PARAMS)
+{
+    rows_body<M, DV, VMODE, G, U>(R32_ARGS);
+}
+template <class M, class DV, int VMODE, int G, int U>
+__global__ void __launch_bounds__(256, 6) taylor_rows_kernel_occ6(R32_PARAMS)
+{
+    rows_body<M, DV, VMODE, G, U>(R32_ARGS);
+}
+
 template <class K>
 int r32_blocks(K kern, const LpTerm &a, int &per_sm)
 {
@@ -212,6 +349,28 @@ int r32_blocks(K kern, const LpTerm &a, int &per_sm)
     const int64_t need = (units + 7) / 8;
     const int64_t cap = (int64_t)qs_num_sms() * per_sm;
     return (int)(need < cap ? (need < 1 ? 1 : need) : cap);
+}
+
+template <class M, class DV, int VMODE, int G>
+int rows_go(const LpTerm &a)
+{
+    constexpr int U = 2;
+    using BE = typename M::BE;
+    static int per_sm[2] = {-1, -1};
+    auto k = a.occ == 1 ? taylor_rows_kernel_occ6<M, DV, VMODE, G, U> : taylor_rows_kernel<M, DV, VMODE, G, U>;
+    int &ps = per_sm[a.occ == 1 ? 1 : 0];
+    if (ps < 0) {
+        int b = 0;
+        QS_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 256, 0));
+        ps = b < 1 ? 1 : b;
+    }
+    const int64_t need = (a.n + (256 / G) - 1) / (256 / G);
+    const int64_t cap = (int64_t)qs_num_sms() * ps;
+    const int blocks = (int)(need < cap ? (need < 1 ? 1 : need) : cap);
+    k<<<blocks, 256, 0, a.st>>>(a.n, (const int32_t *)a.indptr, a.indices, (const DV *)a.data, (const BE *)a.Bin,
+                                (BE *)a.Bout, a.F, a.mu0, a.coeff, a.j, a.tol, (ExpmCtl *)a.ctl);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
 }
 
 template <class M, class DV, int VMODE, int G>
@@ -247,18 +406,21 @@ int r32_g(const LpTerm &a)
     case 1: return r32_go<M, DV, VMODE, 4>(a);
     case 2: return r32_go<M, DV, VMODE, 2>(a);
     case 3: return r32_go<M, DV, VMODE, 8>(a);
+    case 4: return rows_go<M, DV, VMODE, 2>(a);
+    case 5: return rows_go<M, DV, VMODE, 4>(a);
     default: return QS_ERR_ARG;
     }
 }
 
 }  // namespace
 
-// The 32-row single-vector term (a.staged = 1..3: 4, 2 or 8 lanes per row in
-// the gather loop; a.occ = 1: registers capped for 6 blocks per SM, else 4);
-// one vector, int32 indptr and indices.
+// The single-vector terms of this file: a.staged = 1..3 the 32-row kernel
+// with 4, 2 or 8 lanes per row in the gather loop, 4..5 the persistent
+// row-handout kernel with 2 or 4 lanes per row; a.occ = 1: registers capped
+// for 6 blocks per SM, else 4.  One vector, int32 indptr and indices.
 int st_taylor_term(const LpTerm &a)
 {
-    if (a.nvec != 1 || a.idx64 || a.staged < 1 || a.staged > 3) return QS_ERR_ARG;
+    if (a.nvec != 1 || a.idx64 || a.staged < 1 || a.staged > 5) return QS_ERR_ARG;
     if (a.btype == QS_CPF) {
         switch (a.dtype) {
         case QS_PF8: return r32_g<ModePF, pf, 1>(a);

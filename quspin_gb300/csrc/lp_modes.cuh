@@ -93,12 +93,14 @@ struct ModeF32 {
         const float2 v = ld_keep2(reinterpret_cast<const float2 *>(p), pol);
         return BE{v.x, v.y};
     }
+    // explicit rounding everywhere (no contraction), so that every kernel
+    // that uses this mode gives the same bits
     __device__ static void fma(S &acc, S a, S b) { acc = __fmaf_rn(a, b, acc); }
-    __device__ static S merge(S a, S b) { return a + b; }
+    __device__ static S merge(S a, S b) { return __fadd_rn(a, b); }
     __device__ static S fin(S a) { return a; }
-    __device__ static S add(S a, S b) { return a + b; }
-    __device__ static S sub(S a, S b) { return a - b; }
-    __device__ static S mul(S a, S b) { return a * b; }
+    __device__ static S add(S a, S b) { return __fadd_rn(a, b); }
+    __device__ static S sub(S a, S b) { return __fsub_rn(a, b); }
+    __device__ static S mul(S a, S b) { return __fmul_rn(a, b); }
     __device__ static S neg(S a) { return -a; }
     __device__ static float hi(S a) { return a; }
     __device__ static S from_d(double x) { return (float)x; }

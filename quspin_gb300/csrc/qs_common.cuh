@@ -46,6 +46,22 @@ static inline int qs_num_sms()
     return sms;
 }
 
+// Blocks of a grid-stride kernel that are resident on all SMs at once
+// (its occupancy at `threads` threads and no dynamic shared memory), at most
+// `need` and at least 1.  `cache` keeps the per-SM count between calls (one
+// cache per kernel instantiation: a function-local static at the call site).
+template <class K>
+static inline int qs_persistent_grid(K kern, int threads, int64_t need, int &cache)
+{
+    if (cache <= 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, 0) != cudaSuccess || b < 1) b = 1;
+        cache = b;
+    }
+    const int64_t cap = (int64_t)qs_num_sms() * cache;
+    return (int)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
 // complex helpers (plain structs; no std::complex in device code)
 struct cdbl { double x, y; };
 struct cflt { float x, y; };

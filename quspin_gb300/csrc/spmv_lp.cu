@@ -217,9 +217,12 @@ int spmv_go(const SpmvArgs &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
-    spmv_lp_kernel<M, DV, XC, YT, IT, NB, U, CODED><<<grid_rows(a.n, a.G), 256, 0, a.st>>>(
-        a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, a.x, (YT *)a.y, a.nvec, a.a, a.overwrite,
-        a.xnorm);
+    // persistent grid (grid-stride kernel): one wave of resident blocks
+    static int resident = 0;
+    auto k = spmv_lp_kernel<M, DV, XC, YT, IT, NB, U, CODED>;
+    const int blocks = qs_persistent_grid(k, 256, grid_rows(a.n, a.G), resident);
+    k<<<blocks, 256, 0, a.st>>>(a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, a.x, (YT *)a.y,
+                                a.nvec, a.a, a.overwrite, a.xnorm);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }

@@ -185,3 +185,103 @@ class PartitionPredictor:
         m = np.clip(m, 1, 55)
         s = np.maximum(np.ceil(2.0 ** Y[:, 1] - 0.25), 1).astype(np.int64)
         return m, s
+
+
+class NormRatioPredictor:
+    """Learned inputs of Code Fragment 3.1 for one operator (the estimator branch).
+
+    When |a| ||A - mu I||_1 is too large for the exact-norm shortcut
+    (condition 3.13 fails), the reference estimates
+    d_p = ||(a (A - mu I))^p||_1^(1/p) for p = 2 .. 9 with ``onenormest``
+    (html expm_multiply_parallel_core.html:451-463): tens of products with the
+    full matrix.  The ratios d_p / (|a| ||A - mu I||_1) do not depend on a and
+    lie in (0, 1]; this network predicts their logarithms from features that
+    cost nothing beyond the exact 1-norm the constructor computes anyway
+    (the 1-norm, the dimension, the stored entries per row and |mu|), and the
+    selection then runs Code Fragment 3.1 on the predicted d_p.  The outputs
+    are raised by ``MARGIN`` (in log10) so that errors fall on the side of
+    more work.  The plain selection is the fallback: ExpmMultiplyParallel
+    re-runs a product whose Taylor loop used all m* terms of a substep without
+    the stopping test firing with the onenormest (m*, s).  Trained on the GPU
+    by the kernels of csrc/mlp.cu on (features, ratios) of the plain
+    selection over a family of operators (``training_pair``).
+    """
+
+    P = tuple(range(2, 10))
+    MARGIN = 0.03
+
+    def __init__(self, hidden=64, seed=0):
+        self.net = MLP(4, len(self.P), hidden=hidden, layers=3, seed=seed)
+        self.mu = np.zeros(4, np.float32)
+        self.sd = np.ones(4, np.float32)
+
+    @staticmethod
+    def features(one_norm, n, nnz, abs_mu):
+        """[B, 4] features of operators A - mu I: log10 of the exact 1-norm,
+        log10 of the dimension, stored entries per row / 32, log10(1 + |mu|)."""
+        one_norm, n, nnz, abs_mu = (np.atleast_1d(np.asarray(x, np.float64)) for x in (one_norm, n, nnz, abs_mu))
+        return np.column_stack([np.log10(one_norm + 1e-300), np.log10(np.maximum(n, 1.0)),
+                                nnz / np.maximum(n, 1.0) / 32.0, np.log10(1.0 + abs_mu)]).astype(np.float32)
+
+    @classmethod
+    def training_pair(cls, op):
+        """(features [1, 4], log10 ratios [1, 8]) from an ExpmMultiplyParallel
+        whose plain selection ran in the estimator branch."""
+        info = op._norm_info
+        base = info.onenorm()
+        r = np.array([[np.log10(info.d(p) / base) for p in cls.P]], np.float32)
+        A = op.A_device
+        f = cls.features(op._A_1_norm, A.shape[0], A.nnz, abs(complex(op._mu)))
+        return f, r
+
+    def fit(self, feats, log_ratios, epochs=600, lr=3e-3, batch=64, seed=0):
+        self.mu = feats.mean(0)
+        self.sd = feats.std(0) + 1e-3
+        X = D.to_device((feats - self.mu) / self.sd)
+        T = D.to_device(np.asarray(log_ratios, np.float32))
+        return self.net.fit(X, T, epochs=epochs, lr=lr, batch=batch, seed=seed)
+
+    def predict_ratios(self, feats):
+        """[B, 8] predicted d_p / (|a| ||A - mu I||_1), p = 2 .. 9, at most 1."""
+        X = D.to_device(((np.atleast_2d(feats) - self.mu) / self.sd).astype(np.float32))
+        Y = D.to_host(self.net.forward(X)).astype(np.float64)
+        return np.minimum(10.0 ** (Y + self.MARGIN), 1.0)
+
+
+class FixedNormInfo:
+    """Norm information for Code Fragment 3.1 with given d_p (the learned
+    selection): no matrix products."""
+
+    def __init__(self, one_norm, d):
+        self._one = float(one_norm)
+        self._d = dict(d)
+        self.matvecs = 0
+
+    def onenorm(self):
+        return self._one
+
+    def d(self, p):
+        return self._d[p]
+
+    def alpha(self, p):
+        return max(self.d(p), self.d(p + 1))
+
+
+def norm_ratio_training_set(matrices, scale=100.0, seed=0):
+    """(features, log10 ratios) of the plain selection for each device
+    matrix: an ExpmMultiplyParallel with |a| ||A - mu I||_1 = scale (far in
+    the estimator branch; the ratios do not depend on a), onenormest seeded
+    with ``seed`` as the reference's global generator would be."""
+    from .tools import ExpmMultiplyParallel
+    feats, ratios = [], []
+    for A in matrices:
+        np.random.seed(seed)
+        op = ExpmMultiplyParallel(A, a=-1j)
+        if op._A_1_norm == 0:
+            continue
+        np.random.seed(seed)
+        op.set_a(-1j * scale / op._A_1_norm)
+        f, r = NormRatioPredictor.training_pair(op)
+        feats.append(f)
+        ratios.append(r)
+    return np.concatenate(feats), np.concatenate(ratios)

@@ -48,9 +48,12 @@ def _as_device_csr(A):
 
 
 class ExpmMultiplyParallel:
-    """Truncated-Taylor action of e^{aA} (html :115-260)."""
+    """Truncated-Taylor action of e^{aA} (html :115-260).  Beyond the
+    reference's arguments: ``precision`` (see the module docstring) and
+    ``predictor``, a learned.NormRatioPredictor for the (m*, s) selection
+    (see ``set_predictor``)."""
 
-    def __init__(self, A, a=1.0, dtype=None, copy=False, precision="double"):
+    def __init__(self, A, a=1.0, dtype=None, copy=False, precision="double", predictor=None):
         if np.array(a).ndim == 0:
             self._a = a
         else:
@@ -81,6 +84,8 @@ class ExpmMultiplyParallel:
         self._AH = None
         self._mixed = None
         self._bufs = {}
+        self.fallbacks = 0
+        self._predictor = predictor
         self._calculate_partition()
 
     @property
@@ -157,15 +162,48 @@ class ExpmMultiplyParallel:
             return y.reshape(X.shape)
         return f
 
-    def _calculate_partition(self):
+    def set_predictor(self, predictor):
+        """Choose (m*, s) with a learned.NormRatioPredictor whenever the
+        estimator branch of the selection would run (None: always the plain
+        onenormest selection).  A product whose Taylor loop then runs a
+        substep through all m* terms without the stopping test firing is
+        recomputed with the plain selection (``fallbacks`` counts these)."""
+        self._predictor = predictor
+        self._calculate_partition()
+
+    @property
+    def partition_source(self):
+        """'plain' (exact norm or onenormest, as the reference) or 'learned'."""
+        return self.__dict__.get("_partition_source", "plain")
+
+    @property
+    def norm_products(self):
+        """Products with the matrix the last (m*, s) selection made."""
+        info = self.__dict__.get("_norm_info")
+        return 0 if info is None else int(getattr(info, "matvecs", 0))
+
+    def _calculate_partition(self, plain=False):
+        from ._partition import condition_3_13
+        self._partition_source = "plain"
         if np.abs(self._a) * self._A_1_norm == 0:
             self._m_star, self._s = 0, 1
-        else:
-            self._norm_info = LazyOperatorNormInfo(self._shifted_apply(False), self._shifted_apply(True),
-                                                   self._Ad.shape[0], self._A_1_norm, self._a,
-                                                   np.dtype(np.complex128), ell=2,
-                                                   device=(torch.complex128, D.device()))
+            self._norm_info = None
+            return
+        pred = None if plain else self.__dict__.get("_predictor")
+        one = float(np.abs(self._a) * self._A_1_norm)
+        if pred is not None and not condition_3_13(one, 1, 55, 2):
+            from ..learned import FixedNormInfo
+            f = pred.features(self._A_1_norm, self._Ad.shape[0], self._Ad.nnz, abs(complex(self._mu)))
+            r = pred.predict_ratios(f)[0]
+            self._norm_info = FixedNormInfo(one, {p: one * x for p, x in zip(pred.P, r)})
             self._m_star, self._s = fragment_3_1(self._norm_info, 1, self._tol, ell=2)
+            self._partition_source = "learned"
+            return
+        self._norm_info = LazyOperatorNormInfo(self._shifted_apply(False), self._shifted_apply(True),
+                                               self._Ad.shape[0], self._A_1_norm, self._a,
+                                               np.dtype(np.complex128), ell=2,
+                                               device=(torch.complex128, D.device()))
+        self._m_star, self._s = fragment_3_1(self._norm_info, 1, self._tol, ell=2)
 
     # -- application -------------------------------------------------------------
     def _mixed_matrix(self):
@@ -229,7 +267,21 @@ class ExpmMultiplyParallel:
 
     def run_device(self, F, tol=None, work=None):
         """In place e^{aA} F for a complex128 device tensor F of shape (n,) or
-        (n, k).  Returns F.  No host synchronisation."""
+        (n, k).  Returns F.  No host synchronisation, except with a learned
+        (m*, s), where the substep counter is read once to decide on the
+        fallback to the plain selection."""
+        if self.partition_source != "learned":
+            return self._run_device(F, tol, work)
+        saved = F.clone()
+        self._run_device(F, tol, work)
+        if self.nonconverged_substeps:
+            self.fallbacks = self.__dict__.get("fallbacks", 0) + 1
+            self._calculate_partition(plain=True)
+            F.copy_(saved)
+            self._run_device(F, tol, work)
+        return F
+
+    def _run_device(self, F, tol=None, work=None):
         n = self._Ad.shape[0]
         nvec = 1 if F.dim() == 1 else F.shape[1]
         tol = float(self._tol if tol is None else tol)

@@ -42,15 +42,16 @@ def occ_candidates(M, nvec, btype):
 
 
 def r32_candidates(M, nvec, btype):
-    """Shapes of the 32-row single-vector Taylor term (csrc/expm_st.cu; bits
-    20-21 of the launch code: 4, 2 or 8 lanes per row in the gather loop,
-    bits 18-19: 0 / 1 for 4 / 6 resident blocks per SM): one vector, float
-    forms, int32 indices."""
+    """Shapes of the single-vector Taylor terms of csrc/expm_st.cu (bits 20-22
+    of the launch code: 1..3 the 32-row kernel with 4, 2 or 8 lanes per row in
+    the gather loop, 4..5 the persistent row-handout kernel with 2 or 4 lanes
+    per row; bits 18-19: 0 / 1 for 4 / 6 resident blocks per SM): one vector,
+    float forms, int32 indices."""
     if nvec != 1 or btype == _lib.C128 or getattr(M, "idx64", 0):
         return []
     if M.vcode not in (_lib.PF8, _lib.CPF8, _lib.PF8P, _lib.CPF8P, _lib.PF, _lib.CPF, _lib.F32, _lib.C64):
         return []
-    return [(shape, occ) for shape in (1, 2, 3) for occ in (0, 1)]
+    return [(shape, occ) for shape in (1, 2, 3, 4, 5) for occ in (0, 1)]
 
 
 def _time(fn, reps=5):
@@ -116,7 +117,8 @@ def tune_taylor(M, nvec, btype):
     cands += [(G, U, occ << 2) for G, U in occ_candidates(M, nvec, btype) for occ in (1, 2)]
     if getattr(M, "vcode", None) in (_lib.PF8P, _lib.CPF8P):
         cands = []                 # the packed form runs only in the 32-row kernel
-    cands += [({1: 4, 2: 2, 3: 8}[shape], 2, (shape << 4) | (occ << 2)) for shape, occ in r32_candidates(M, nvec, btype)]
+    cands += [({1: 4, 2: 2, 3: 8, 4: 2, 5: 4}[shape], 2, (shape << 4) | (occ << 2))
+              for shape, occ in r32_candidates(M, nvec, btype)]
     for G, U, ch in cands:
         code = encode(G, U) | (ch << 16)
 

@@ -122,8 +122,8 @@ def test_r32_candidates_need_one_vector_float_forms():
 
     def M(vcode, idx64=0):
         return type("M", (), {"idx64": idx64, "vcode": vcode})()
-    assert r32_candidates(M(_lib.PF8P), 1, _lib.CPF) == [(s, o) for s in (1, 2, 3) for o in (0, 1)]
-    assert len(r32_candidates(M(_lib.PF8), 1, _lib.CPF)) == 6
+    assert r32_candidates(M(_lib.PF8P), 1, _lib.CPF) == [(s, o) for s in (1, 2, 3, 4, 5) for o in (0, 1)]
+    assert len(r32_candidates(M(_lib.PF8), 1, _lib.CPF)) == 10
     assert r32_candidates(M(_lib.PF8), 2, _lib.CPF) == []
     assert r32_candidates(M(_lib.PF8), 1, _lib.C128) == []
     assert r32_candidates(M(_lib.PF8, idx64=1), 1, _lib.CPF) == []

@@ -89,3 +89,31 @@ def test_driven_learned_matches_plain(cuda):
     for i in range(nsteps):
         W = expm_multiply(-1j * dt * H.tocsr(time=dt * (i + 0.5)), W)
     assert np.linalg.norm(wp - W) <= 1e-12 * np.linalg.norm(W)
+
+
+def test_driven_fallback_restores_plain(cuda):
+    """A predictor that returns far too small (m*, s) makes the Taylor loop run
+    substeps through all m* terms without the stopping test firing; every such
+    segment is re-run from its saved state with the plain selection
+    (tools/driven.py), so the result equals the plain run's."""
+    from quspin_gb300.learned import PartitionPredictor
+    from quspin_gb300.tools.driven import DrivenEvolution
+
+    class TooSmall(PartitionPredictor):
+        def predict(self, feats):
+            k = np.atleast_2d(feats).shape[0]
+            return np.full(k, 2, np.int64), np.ones(k, np.int64)
+
+    H, _ = _driven()
+    ev = DrivenEvolution(H, nvec=2)
+    rng = np.random.default_rng(5)
+    V = rng.normal(size=(H.Ns, 2)) + 1j * rng.normal(size=(H.Ns, 2))
+    V /= np.linalg.norm(V, axis=0)
+    dt, nsteps = 0.05, 20
+    Fp = torch.tensor(V, device="cuda")
+    Fl = Fp.clone()
+    ev.run(Fp, 0.0, dt, nsteps, mode="plain")
+    ev.fallbacks = 0
+    ev.run(Fl, 0.0, dt, nsteps, mode="learned", predictor=TooSmall(n_coeffs=1), segment=10)
+    assert ev.fallbacks == 2
+    assert np.array_equal(Fl.cpu().numpy().view(np.float64), Fp.cpu().numpy().view(np.float64))

@@ -1,5 +1,6 @@
-"""The 32-row single-vector Taylor term (csrc/expm_st.cu) against the
-row-handout term (csrc/expm_lp.cu) on the same inputs: one term gives
+"""The single-vector Taylor terms of csrc/expm_st.cu (the 32-row kernel and
+the persistent row-handout kernel) against the row-handout term of
+csrc/expm_lp.cu on the same inputs: one term gives
 bit-identical B, F and stopping-test norm for every value form (coded,
 coded with the codes packed into the column words, one pair per nonzero,
 complex coded, and the complex64 form) and every lane count, on a matrix
@@ -68,7 +69,7 @@ def test_r32_term_bitwise_equal_to_row_handout(cuda, complex_vals):
     coded = Ad.paired(coded=True)
     assert coded.coded
     forms = [coded, coded.packed(), Ad.paired(coded=False)]
-    for G, shape in ((4, 1), (2, 2), (8, 3)):
+    for G, shape in ((4, 1), (2, 2), (8, 3), (2, 4), (4, 5)):
         ref = _term(coded, encode(G, 2), Bp, F0, _lib.CPF)
         for M in forms:
             for occ in (0, 1):
@@ -78,7 +79,7 @@ def test_r32_term_bitwise_equal_to_row_handout(cuda, complex_vals):
     # complex64 form: float32 / complex64 values, complex64 B
     M32 = Ad.astype(np.complex64 if complex_vals else np.float32)
     B32 = v.to(torch.complex64)
-    for G, shape in ((4, 1), (2, 2)):
+    for G, shape in ((4, 1), (2, 2), (2, 4), (4, 5)):
         ref = _term(M32, encode(G, 2), B32, F0, _lib.C64)
         out = _term(M32, encode(G, 2) | (shape << 20), B32, F0, _lib.C64)
         assert _same(out[0], ref[0]) and _same(out[1], ref[1]) and out[2] == ref[2]
@@ -95,7 +96,8 @@ def test_r32_evolution_bitwise_equal(cuda):
     v = rng.normal(size=n) + 1j * rng.normal(size=n)
     v /= np.linalg.norm(v)
     out = []
-    for packed, code in ((False, encode(4, 2)), (False, encode(4, 2) | (1 << 20)), (True, encode(4, 2) | (1 << 20))):
+    for packed, code in ((False, encode(4, 2)), (False, encode(4, 2) | (1 << 20)), (True, encode(4, 2) | (1 << 20)),
+                         (True, encode(4, 2) | (5 << 20) | (1 << 18))):
         op = ExpmMultiplyParallel(DeviceCSR.from_scipy(A), a=-0.8j)
         P = op.A_device.paired()
         M = P.packed() if packed else P
@@ -104,5 +106,5 @@ def test_r32_evolution_bitwise_equal(cuda):
         F = torch.tensor(v, device="cuda")
         op.run_device(F)
         out.append(F.cpu().numpy())
-    assert np.array_equal(out[0].view(np.int64), out[1].view(np.int64))
-    assert np.array_equal(out[0].view(np.int64), out[2].view(np.int64))
+    for o in out[1:]:
+        assert np.array_equal(out[0].view(np.int64), o.view(np.int64))
