@@ -506,7 +506,19 @@ def cpu_baseline(A, v, op, budget_s=12.0):
     while ev.k < op.s and (ev.k == 0 or time.perf_counter() - t0 < budget_s):
         ev.substep()
     T = time.perf_counter() - t0
+    # the restated OpenMP CSR product (SpMV of hamiltonian.dot) on the same matrix
+    x = np.ascontiguousarray(v, dtype=np.complex128)
+    y = np.empty_like(x)
+    O.csr_matvec(A, x, out=y)
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.csr_matvec(A, x, out=y)
+    t_spmv = (time.perf_counter() - t0) / reps
+    n, nnz = A.shape[0], A.nnz
     return {"value": ev.k / op.s / T, "unit": "evolutions/s", "cores": int(O.num_threads()), "kind": "port",
+            "spmv": {"ms": 1e3 * t_spmv, "gbs": spmv_bytes(n, nnz, vb=8) / t_spmv / 1e9,
+                     "bytes": "algorithmic, float64 values and int32 indices"},
             "sample": "the first {} of the {} substeps of this evolution ({} Taylor terms, real coefficients, shift "
                       "and stopping test) in the oracle's OpenMP loop, {:.2f} s; evolutions/s = substeps / {} / "
                       "seconds".format(ev.k, op.s, sum(ev.terms), T, op.s),
@@ -994,8 +1006,30 @@ def run_lanczos(args):
         res[spmv] = {"E0": float(E[0]), "E1": float(E[1]), "seconds": el, "iterations_per_s": m / el}
         del Q
     res["double"]["abs_E0_error_vs_ieee"] = abs(res["double"]["E0"] - res["ieee"]["E0"])
+    # the reference's recurrence without per-step reorthogonalisation (its
+    # default), GPU and the oracle's numpy restatement over the OpenMP CSR
+    # product on the host cores, a bounded number of iterations each
+    lanczos_full(A, v0, 10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lanczos_full(A, v0, m)
+    torch.cuda.synchronize()
+    gpu_plain = m / (time.perf_counter() - t0)
+    cpu = {}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        Ah = A.tocsr()
+        mc = 20
+        vh = v0.cpu().numpy()
+        t0 = time.perf_counter()
+        O.lanczos_full(lambda x: O.csr_matvec(Ah, x).real, np.float64, vh, mc)
+        tc = time.perf_counter() - t0
+        cpu = {"iterations_per_s": mc / tc, "cores": int(O.num_threads()), "kind": "port",
+               "sample": "{} iterations of the oracle's restatement of _lanczos_utils.lanczos_full (numpy "
+                         "recurrence, OpenMP CSR product), {:.2f} s".format(mc, tc)}
     out = {"workload": "j1j2_chain_L{}_lanczos_200_reorth".format(L), "Ns": A.shape[0], "nnz": A.nnz,
-           "build_s": t_build, "m": m, "spmv_ieee": res["ieee"], "spmv_float_pairs": res["double"]}
+           "build_s": t_build, "m": m, "spmv_ieee": res["ieee"], "spmv_float_pairs": res["double"],
+           "no_reorth": {"gpu_iterations_per_s": gpu_plain, "cpu_baseline": cpu}}
     print(json.dumps(out))
 
 

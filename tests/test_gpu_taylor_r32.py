@@ -15,19 +15,32 @@ pytestmark = pytest.mark.gpu
 
 
 def _matrix(n=70001, complex_vals=False, seed=0):
+    """Hermitian matrix with few distinct values (so that it codes): unique
+    upper-triangle pairs with values from a small set, their conjugate
+    transposes and a diagonal from a small set; one empty row, one long row."""
     rng = np.random.default_rng(seed)
-    nnz = 24 * n
-    r, c = rng.integers(0, n, nnz), rng.integers(0, n, nnz)
-    vals = rng.choice(np.array([0.5, -0.5, 0.25, 1.0, -1.5, 0.7071067811865476]), nnz)
+    m = 12 * n
+    r, c = rng.integers(0, n, m), rng.integers(0, n, m)
+    lo, hi = np.minimum(r, c), np.maximum(r, c)
+    keep = lo < hi
+    key = np.unique(lo[keep].astype(np.int64) * n + hi[keep])
+    long_row = n // 2
+    key = np.unique(np.concatenate([key, np.minimum(long_row, np.arange(0, n, 37)) * n
+                                    + np.maximum(long_row, np.arange(0, n, 37))]))
+    key = key[(key // n) < (key % n)]
+    empty = n // 3
+    key = key[(key // n != empty) & (key % n != empty)]
+    rr, cc = key // n, key % n
+    vals = np.array([0.5, -0.5, 0.25, 1.0, -1.5, 0.7071067811865476])
     if complex_vals:
-        vals = vals * np.exp(1j * rng.choice(np.array([0.0, 0.5, 1.0]), nnz))
-    A = sp.csr_matrix((vals, (r, c)), shape=(n, n))
-    A = sp.csr_matrix(A + A.conj().T)
-    A = A.tolil()
-    A[n // 3, :] = 0                                       # an empty row
-    A[n // 2, np.arange(0, n, 37)] = 0.5                   # a long row
-    A = sp.csr_matrix(A)
-    A.sum_duplicates()
+        vals = vals * np.exp(1j * np.array([0.0, 0.5, 1.0, 0.5, 0.0, 1.0]))
+    v = rng.choice(vals, key.size)
+    d = rng.choice(np.array([0.0, 0.3, -1.2]), n)
+    d[empty] = 0.0
+    U = sp.csr_matrix((v, (rr, cc)), shape=(n, n))
+    A = sp.csr_matrix(U + U.conj().T + sp.diags(d))
+    A.eliminate_zeros()
+    assert A[empty].nnz == 0 and A[long_row].nnz > 1000
     return A
 
 
