@@ -327,9 +327,8 @@ def gather_probe(A, F, reps=10):
     for G in (2, 4, 8):
         for bps in (6, 8):
             def run():
-                rc = probe(ctypes.c_int64(A.shape[0]), ctypes.c_void_p(D.ptr(A.indptr)),
-                           ctypes.c_void_p(D.ptr(A.indices)), ctypes.c_void_p(D.ptr(F)), ctypes.c_void_p(D.ptr(y)),
-                           G, bps, ctypes.c_void_p(D.stream()))
+                rc = probe(ctypes.c_int64(A.shape[0]), D.ptr(A.indptr), D.ptr(A.indices), D.ptr(F), D.ptr(y),
+                           ctypes.c_int(G), ctypes.c_int(bps), D.stream())
                 if rc:
                     raise RuntimeError("bench_gather_probe returned {}".format(rc))
             for _ in range(2):
@@ -661,6 +660,7 @@ def run_ours(args, rank, ws):
     traffic, traffic_note = profile_traffic(taylor_kernel_name(group))
     P, _ = op._operand(1)           # the operand form the evolution runs on (coded, or codes packed in the indices)
     vb = P.value_bytes
+    vb_mv = A.paired().value_bytes  # hamiltonian.dot's product reads the coded operand
     probe = gather_probe(A, v_dev)
     tb = taylor_term_bytes(n, nnz, vb=vb)
     achieved = tb / t_term / 1e9
@@ -695,8 +695,9 @@ def run_ours(args, rank, ws):
                          "ms": probe[0], "lanes_per_row": probe[1], "blocks_per_sm": probe[2],
                          "gathers_per_s": nnz / (probe[0] / 1e3),
                          "kernel_time_over_probe": 1e3 * t_term / probe[0]},
-                     "spmv_gbs": spmv_bytes(n, nnz, vb=vb) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
-                     "spmm8_gbs": spmv_bytes(n, nnz, 8, vb=vb) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
+                     "spmv_gbs": spmv_bytes(n, nnz, vb=vb_mv) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
+                     "spmm8_gbs": spmv_bytes(n, nnz, 8, vb=vb_mv) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
+                     "spmv_value_bytes_per_nonzero": vb_mv,
                      "library_spmv": lib_ctx},
         "gpu_launches": int(args.steps * launches_per_evolution),
         "clocks": clk.summary(),
