@@ -27,10 +27,12 @@
 // lane holds the row sum, lanes 0 and 1 write the real and imaginary part of
 // the new term and of F (two FP64 adds each for the paired form), so the
 // FP64 pipe sees a handful of fully used instructions per row instead of
-// two per nonzero.  The stopping test is evaluated on IEEE double values: the
-// squared modulus of each new term element and each F element is formed in
-// FP64 from the exact double value of the float pair (the many-vector row
-// sums of moduli take the square root with sqrt_newton).
+// two per nonzero.  The stopping test: with one column, the squared modulus
+// of each new term element and each F element is formed in FP64 from the
+// exact double value of the float pair; with several columns the row sums of
+// moduli are formed in float-pair arithmetic (squares to 2^-48, square roots
+// to about 2^-44 relative: pf_sqrt), since a square root per element in FP64
+// would load GB300's narrow FP64 pipe with a dozen instructions per element.
 #include "qs_common.cuh"
 #include <type_traits>
 #include "expm_ctl.cuh"
@@ -143,6 +145,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
         const S cm_re = s_cm[2 * sec];
         const S cm_x = comp ? s_cm[2 * sec + 1] : M::neg(s_cm[2 * sec + 1]);
         double rbn = 0.0, rfn = 0.0;
+        pf rbp{0.f, 0.f}, rfp{0.f, 0.f};     // many columns: row sums of moduli as pairs
         BE bo_pre{M::zero(), M::zero()};
         double f_pre = 0.0;
         if (NB == 1 && writer) {
@@ -193,7 +196,9 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                 const S bo_c = comp ? bo.im : bo.re, bo_o = comp ? bo.re : bo.im;
                 const S mine = M::sub(M::add(M::mul(cf_re, acc_c), M::mul(cf_x, acc_o)),
                                       M::add(M::mul(cm_re, bo_c), M::mul(cm_x, bo_o)));
-                // squared moduli in FP64, scaled by 2^-bexp
+                // moduli scaled by 2^-bexp: one column, squared moduli in FP64 (the square
+                // root is taken once, at the end); several columns, row sums of moduli
+                // formed in float-pair arithmetic (pf_sqrt)
                 double md = 0.0, fs = 0.0;
                 if (writer) {
                     M::st_comp(Bout + e, comp, mine);
@@ -201,20 +206,29 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                     double fv = NB == 1 ? f_pre : __ldcs(fp);
                     fv = M::add_to(fv, mine, bexp);
                     __stcs(fp, fv);
-                    md = M::to_d(mine, 0);
+                    if (NB == 1) md = M::to_d(mine, 0);
                     fs = fv * s_inv;
                 }
-                double nb2 = __dmul_rn(md, md), f2 = __dmul_rn(fs, fs);
-                nb2 = __dadd_rn(nb2, __shfl_xor_sync(0xffffffffu, nb2, 1));
-                f2 = __dadd_rn(f2, __shfl_xor_sync(0xffffffffu, f2, 1));
-                if (NB == 1) {
-                    rbn = nb2;          // one column: squared moduli, square root once at the end
+                if constexpr (NB == 1) {
+                    double nb2 = __dmul_rn(md, md), f2 = __dmul_rn(fs, fs);
+                    nb2 = __dadd_rn(nb2, __shfl_xor_sync(0xffffffffu, nb2, 1));
+                    f2 = __dadd_rn(f2, __shfl_xor_sync(0xffffffffu, f2, 1));
+                    rbn = nb2;
                     rfn = f2;
                 } else {
-                    rbn += sqrt_newton(nb2);
-                    rfn += sqrt_newton(f2);
+                    const pf bm = writer ? to_pair(mine) : pf{0.f, 0.f};
+                    const pf fm = writer ? pair_of_double(fs) : pf{0.f, 0.f};
+                    pf b2 = pf_mul(bm, bm), f2 = pf_mul(fm, fm);
+                    b2 = pf_add(b2, shfl_xor_pair(b2, 1));
+                    f2 = pf_add(f2, shfl_xor_pair(f2, 1));
+                    rbp = pf_add(rbp, pf_sqrt(b2));
+                    rfp = pf_add(rfp, pf_sqrt(f2));
                 }
             }
+        }
+        if constexpr (NB > 1) {
+            rbn = pf_to_double_scaled(rbp, 0);
+            rfn = pf_to_double_scaled(rfp, 0);
         }
         if (chunk_outer && writer && lane == 0) {
             double2 acc = sw == 0 ? make_double2(0.0, 0.0) : rownorm[r];

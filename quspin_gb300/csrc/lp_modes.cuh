@@ -164,28 +164,37 @@ __device__ __forceinline__ double pow2(int k)   // 2^k for |k| <= 1000
     return __hiloint2double((1023 + k) << 20, 0);
 }
 
-// Square root of a double for the stopping-test norms of the many-vector
-// terms, with FP64 accuracy at a few FP64 instructions: x = m 4^k with m in
-// [1, 4) (exact exponent arithmetic), y0 ~ 1/sqrt(m) from the FP32
-// reciprocal square root, one Newton-Raphson step y1 = y0 (3 - m y0^2) / 2 for
-// 1/sqrt(m) (relative error about 2^-44), s = m y1 and one Newton step for
-// the root itself, s + y1 (m - s^2) / 2, which squares the error again, so
-// the result is within a few ulps of sqrt(x).  0 for x <= 0 or NaN; x = inf
-// gives inf.
-__device__ __forceinline__ double sqrt_newton(double x)
+// Moduli for the stopping test of the many-vector terms, in float-pair
+// arithmetic on the FP32 pipe (GB300's FP64 pipe is a small fraction of its
+// FP32 rate, and a square root in FP64 costs a dozen FP64 instructions per
+// vector element).  pf_mul squares a pair with an error of order 2^-48
+// relative; pf_sqrt takes the correctly rounded FP32 root of the high part
+// and one correction with the exact FMA remainder, so the root of a pair is
+// accurate to about 2^-44 relative.
+__device__ __forceinline__ pf to_pair(pf v) { return v; }
+__device__ __forceinline__ pf to_pair(float v) { return pf{v, 0.f}; }
+
+__device__ __forceinline__ pf shfl_xor_pair(pf a, int o)
 {
-    if (!(x > 0.0)) return 0.0;
-    const int hi = __double2hiint(x);
-    const int E = (hi >> 20) & 0x7ff;
-    if (E == 0x7ff) return x;
-    if (E == 0) return sqrt_newton(x * 0x1p104) * 0x1p-52;   // subnormal: scale into the normal range
-    const int k = (E - 1023) >> 1;                          // floor((E - 1023) / 2)
-    const double m = __hiloint2double(hi - (k << 21), __double2loint(x));   // x 4^-k, in [1, 4)
-    const double y0 = (double)rsqrtf((float)m);
-    const double y1 = y0 * fma(-0.5 * m, y0 * y0, 1.5);
-    double s = m * y1;
-    s = fma(0.5 * y1, fma(-s, s, m), s);
-    return s * __hiloint2double((1023 + k) << 20, 0);
+    return pf{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
 }
+
+// a double as an unevaluated pair of floats (high part by truncation on the
+// bit pattern, one FP64 subtraction for the rest; O(1) inputs)
+__device__ __forceinline__ pf pair_of_double(double x)
+{
+    const float h = d2f_scaled(x, 0);
+    return pf{h, d2f_scaled(x - f2d_scaled(h, 0), 0)};
+}
+
+__device__ __forceinline__ pf pf_sqrt(pf x)
+{
+    if (!(x.h > 0.f)) return pf{0.f, 0.f};
+    const float s = __fsqrt_rn(x.h);
+    const float r = __fadd_rn(__fmaf_rn(-s, s, x.h), x.l);     // x - s^2 (the FMA remainder is exact)
+    const float c = __fmul_rn(__fmul_rn(0.5f, r), __frcp_rn(s));
+    return pf_norm(pf{s, c});
+}
+
 
 }  // namespace
