@@ -676,7 +676,9 @@ def run_ours(args, rank, ws):
     traffic, traffic_note = profile_traffic(taylor_kernel_name(group))
     P, _ = op._operand(1)           # the operand form the evolution runs on (coded, or codes packed in the indices)
     vb = P.value_bytes
-    vb_mv = A.paired().value_bytes  # hamiltonian.dot's product reads the coded operand
+    # hamiltonian.dot's product reads the coded operand, in its packed form where that applies
+    Pmv = A.paired()
+    vb_mv = (Pmv.packed() or Pmv).value_bytes if Pmv.coded else Pmv.value_bytes
     probe = gather_probe(A, v_dev)
     tb = taylor_term_bytes(n, nnz, vb=vb)
     achieved = tb / t_term / 1e9

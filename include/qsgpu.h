@@ -132,9 +132,12 @@ int qs_csr_matvec(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const
                   const void *d_data, int dtype, const void *d_x, int xtype, void *d_y, int64_t nvec, double a_re,
                   double a_im, int overwrite, int group, void *stream);
 /* Paired-single form of qs_csr_matvec for float64 / complex128 x and y: the
- * values split by qs_split_pairs (pdtype 4 / 5), x scaled by a power of two
- * and split into d_xs (n*nvec*8 or 16 bytes of scratch; d_norm: 8 bytes),
- * products and row sums in FP32 instructions with 48-bit significands. */
+ * values split by qs_split_pairs (pdtype 4 / 5), coded (6 / 7: a table of
+ * 256 pairs, then one code byte per nonzero) or packed (8 / 9: d_indices
+ * holds col << 8 | code with col < 2^23, d_pdata the table only), x scaled
+ * by a power of two and split into d_xs (n*nvec*8 or 16 bytes of scratch;
+ * d_norm: 8 bytes), products and row sums in FP32 instructions with 48-bit
+ * significands. */
 int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                         const void *d_pdata, int pdtype, const void *d_x, int xtype, void *d_y, int64_t nvec,
                         double a_re, double a_im, int overwrite, int group, void *d_xs, void *d_norm, void *stream);
@@ -261,8 +264,15 @@ int qs_lanczos_alpha(int64_t n, int cplx, double *d_r, const double *d_v, const 
                      double *d_a_out, double *d_scratch, void *d_ctl, void *stream);
 int qs_lanczos_beta(int64_t n2, double *d_r, const double *d_a, const double *d_q, int do_axpy, double *d_b_out,
                     double eps, int i, double *d_scratch, void *d_ctl, void *stream);
+/* Classical Gram-Schmidt against the rows Q[0..nk-1] (row stride ldq in
+ * elements), `passes` times; the adaptive form runs a further pass only
+ * while a pass removes more than 1 - 1/sqrt(2) of the norm of r (at most
+ * max_passes), decided on the device.  d_scratch: at least
+ * qs_lanczos_reorth_scratch_doubles(nk) doubles. */
 int qs_lanczos_reorth(int64_t n, int cplx, int nk, const double *d_Q, int64_t ldq, double *d_r, int passes,
                       double *d_scratch, void *d_ctl, void *stream);
+int qs_lanczos_reorth_adaptive(int64_t n, int cplx, int nk, const double *d_Q, int64_t ldq, double *d_r,
+                               int max_passes, double *d_scratch, void *d_ctl, void *stream);
 int qs_lanczos_lincomb(int64_t n_el, int nk, const double *d_c, int cplx_c, const double *d_Q, int64_t ldq,
                        int cplx_q, double *d_out, void *stream);
 

@@ -110,6 +110,7 @@ _SIGS = {
     "qs_lanczos_alpha": (_i, [_i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qs_lanczos_beta": (_i, [_i64, _vp, _vp, _vp, _i, _vp, _d, _i, _vp, _vp, _vp]),
     "qs_lanczos_reorth": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i, _vp, _vp, _vp]),
+    "qs_lanczos_reorth_adaptive": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i, _vp, _vp, _vp]),
     "qs_lanczos_lincomb": (_i, [_i64, _i, _vp, _i, _vp, _i64, _i, _vp, _vp]),
     "qs_block_inner_scratch_doubles": (_i64, [_i64, _i, _i, _i]),
     "qs_block_inner": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i64, _i, _i, _i, _vp, _vp, _vp]),

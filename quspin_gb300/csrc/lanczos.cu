@@ -124,72 +124,112 @@ __global__ void lz_axpy_norm_kernel(int64_t n2, double *__restrict__ r, const do
 }
 
 // ---- full reorthogonalisation ---------------------------------------------
-// h[k] = <Q[k], r> for k < nk: per-block partials part[blk * nk + k]
-#define RO_ROWS 8
-__global__ void lz_gemv_t_kernel(int64_t n, int cplx, int nk, const double *__restrict__ Q, int64_t ldq,
-                                 const double *__restrict__ r, double *__restrict__ part, const LzCtl *ctl)
+// h[k] = <Q[k], r> for k < nk.  Each thread keeps 16 FP64 accumulators: 16
+// rows (real) or 8 rows x (re, im) (complex).  A warp reduces them with a
+// reduce-scatter butterfly (16 adds per lane instead of 5 per accumulator),
+// which matters here because the FP64 pipe, not HBM, bounds this kernel.
+// Per-block partials go to part[a * nb + blk], a = k (real) or 2k + c
+// (complex), so that the finish kernel reads them contiguously.
+#define RO_ACC 16
+
+// sum over the 32 lanes of v[0..15]; returns the full warp sum of
+// accumulator lane >> 1 (the same value in lanes 2a and 2a + 1)
+__device__ __forceinline__ double warp_reduce_scatter16(double (&v)[RO_ACC], int lane)
 {
-    if (ctl->done) return;
-    __shared__ double sh[RO_ROWS][2][LZ_THREADS / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int k0 = 0; k0 < nk; k0 += RO_ROWS) {
-        double sr[RO_ROWS], si[RO_ROWS];
+    double w[8], x[4], y[2];
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
 #pragma unroll
-        for (int t = 0; t < RO_ROWS; t++) { sr[t] = 0.0; si[t] = 0.0; }
+    for (int j = 0; j < 8; j++) {
+        const double send = b4 ? v[j] : v[j + 8], keep = b4 ? v[j + 8] : v[j];
+        w[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const double send = b3 ? w[j] : w[j + 4], keep = b3 ? w[j + 4] : w[j];
+        x[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const double send = b2 ? x[j] : x[j + 2], keep = b2 ? x[j + 2] : x[j];
+        y[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    const double send = b1 ? y[0] : y[1], keep = b1 ? y[1] : y[0];
+    double z = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    return z + __shfl_xor_sync(0xffffffffu, z, 1);
+}
+
+template <bool CPLX>
+__global__ void __launch_bounds__(LZ_THREADS, 4)
+lz_gemv_t_kernel(int64_t n, int nk, const double *__restrict__ Q, int64_t ldq, const double *__restrict__ r,
+                 double *__restrict__ part, const LzCtl *ctl, const double *skip)
+{
+    if (ctl->done || (skip && *skip != 0.0)) return;
+    constexpr int R = CPLX ? RO_ACC / 2 : RO_ACC;   // rows per group
+    __shared__ double sh[RO_ACC][LZ_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nb = gridDim.x;
+    for (int k0 = 0; k0 < nk; k0 += R) {
+        const int rows = nk - k0 < R ? nk - k0 : R;
+        double acc[RO_ACC];
+#pragma unroll
+        for (int t = 0; t < RO_ACC; t++) acc[t] = 0.0;
+        const double *q0 = Q + (int64_t)k0 * ldq;
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-            if (cplx) {
-                double rr = r[2 * i], ri = r[2 * i + 1];
+            if constexpr (CPLX) {
+                const double rr = r[2 * i], ri = r[2 * i + 1];
 #pragma unroll
-                for (int t = 0; t < RO_ROWS; t++) {
-                    if (k0 + t < nk) {
-                        const double *qk = Q + (int64_t)(k0 + t) * ldq;
-                        double qr = qk[2 * i], qi = qk[2 * i + 1];
-                        sr[t] += qr * rr + qi * ri;
-                        si[t] += qr * ri - qi * rr;
+                for (int t = 0; t < R; t++) {
+                    if (t < rows) {
+                        const double qr = q0[t * ldq + 2 * i], qi = q0[t * ldq + 2 * i + 1];
+                        acc[2 * t] += qr * rr + qi * ri;
+                        acc[2 * t + 1] += qr * ri - qi * rr;
                     }
                 }
             } else {
-                double rr = r[i];
+                const double rr = r[i];
 #pragma unroll
-                for (int t = 0; t < RO_ROWS; t++)
-                    if (k0 + t < nk) sr[t] += Q[(int64_t)(k0 + t) * ldq + i] * rr;
+                for (int t = 0; t < R; t++)
+                    if (t < rows) acc[t] += q0[t * ldq + i] * rr;
             }
         }
-#pragma unroll
-        for (int t = 0; t < RO_ROWS; t++) {
-            double a = wsum(sr[t]), b = wsum(si[t]);
-            if (lane == 0) { sh[t][0][w] = a; sh[t][1][w] = b; }
-        }
+        const double s = warp_reduce_scatter16(acc, lane);
+        if (!(lane & 1)) sh[lane >> 1][w] = s;
         __syncthreads();
-        if (threadIdx.x < RO_ROWS && k0 + threadIdx.x < nk) {
-            double a = 0.0, b = 0.0;
-            for (int ww = 0; ww < LZ_THREADS / 32; ww++) { a += sh[threadIdx.x][0][ww]; b += sh[threadIdx.x][1][ww]; }
-            int64_t o = ((int64_t)blockIdx.x * nk + k0 + threadIdx.x) * 2;
-            part[o] = a;
-            part[o + 1] = b;
+        if (threadIdx.x < RO_ACC) {
+            const int a = threadIdx.x;
+            if ((CPLX ? a >> 1 : a) < rows) {
+                double tot = 0.0;
+                for (int ww = 0; ww < LZ_THREADS / 32; ww++) tot += sh[a][ww];
+                part[((int64_t)(CPLX ? 2 * k0 : k0) + a) * nb + blockIdx.x] = tot;
+            }
         }
         __syncthreads();
     }
 }
 
-// h[k] = sum over blocks of part[blk * nk + k] (fixed order)
-__global__ void lz_gemv_t_finish(int nb, int nk, const double *__restrict__ part, double *__restrict__ h,
-                                 const LzCtl *ctl)
+// h[k] = sum over blocks of the partials (one warp per accumulator, fixed
+// order: strided lane sums, then a butterfly); real: h[2k + 1] = 0
+__global__ void lz_gemv_t_finish(int nb, int nk, int cplx, const double *__restrict__ part, double *__restrict__ h,
+                                 const LzCtl *ctl, const double *skip)
 {
-    if (ctl->done) return;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nk; k += gridDim.x * blockDim.x) {
-        double a = 0.0, b = 0.0;
-        for (int blk = 0; blk < nb; blk++) { a += part[((int64_t)blk * nk + k) * 2]; b += part[((int64_t)blk * nk + k) * 2 + 1]; }
-        h[2 * k] = a;
-        h[2 * k + 1] = b;
+    if (ctl->done || (skip && *skip != 0.0)) return;
+    const int a = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (a >= (cplx ? 2 * nk : nk)) return;
+    const double *p = part + (int64_t)a * nb;
+    double s = 0.0;
+    for (int b = lane; b < nb; b += 32) s += p[b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        if (cplx) h[a] = s;
+        else { h[2 * a] = s; h[2 * a + 1] = 0.0; }
     }
 }
 
 // r -= sum_k h[k] Q[k]
 __global__ void lz_gemv_n_kernel(int64_t n, int cplx, int nk, const double *__restrict__ Q, int64_t ldq,
-                                 const double *__restrict__ h, double *__restrict__ r, const LzCtl *ctl)
+                                 const double *__restrict__ h, double *__restrict__ r, const LzCtl *ctl,
+                                 const double *skip)
 {
-    if (ctl->done) return;
+    if (ctl->done || (skip && *skip != 0.0)) return;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (cplx) {
             double ar = 0.0, ai = 0.0;
@@ -246,9 +286,46 @@ extern "C" int qs_lanczos_beta(int64_t n2, double *r, const double *aptr, const 
     return QS_OK;
 }
 
+// Scratch: per-block partials of h (2 * LZ_BLOCKS_MAX * nk), h (2 nk), the
+// pass-control state (2) and the norm partials (LZ_BLOCKS_MAX).
 extern "C" int64_t qs_lanczos_reorth_scratch_doubles(int nk)
 {
-    return (int64_t)2 * LZ_BLOCKS_MAX * (nk > 0 ? nk : 1) + 2 * (int64_t)(nk > 0 ? nk : 1);
+    const int64_t k = nk > 0 ? nk : 1;
+    return (int64_t)2 * LZ_BLOCKS_MAX * k + 2 * k + 2 + LZ_BLOCKS_MAX;
+}
+
+// Pass control of the adaptive reorthogonalisation.  state[0]: squared norm
+// of r before the last pass; state[1]: 1 once a pass kept at least 1/sqrt(2)
+// of the norm (then r is orthogonal to the rows to working precision and
+// the remaining passes return at once).  first: record the norm of the
+// incoming r and clear the flag.
+__global__ void lz_dgks_kernel(int nb, const double *__restrict__ partial, double *state, int first, const LzCtl *ctl)
+{
+    if (ctl->done) return;
+    if (!first && state[1] != 0.0) return;
+    double s = 0.0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) s += partial[k];
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        if (first) {
+            state[0] = s;
+            state[1] = 0.0;
+        } else if (s >= 0.5 * state[0]) {
+            state[1] = 1.0;
+        } else {
+            state[0] = s;
+        }
+    }
+}
+
+static void reorth_pass(cudaStream_t st, int nb, int64_t n, int cplx, int nk, const double *Q, int64_t ldq, double *r,
+                        double *part, double *h, const LzCtl *ctl, const double *skip)
+{
+    if (cplx) lz_gemv_t_kernel<true><<<nb, LZ_THREADS, 0, st>>>(n, nk, Q, 2 * ldq, r, part, ctl, skip);
+    else lz_gemv_t_kernel<false><<<nb, LZ_THREADS, 0, st>>>(n, nk, Q, ldq, r, part, ctl, skip);
+    const int nacc = cplx ? 2 * nk : nk;
+    lz_gemv_t_finish<<<(nacc + 7) / 8, 256, 0, st>>>(nb, nk, cplx, part, h, ctl, skip);
+    lz_gemv_n_kernel<<<nb, LZ_THREADS, 0, st>>>(n, cplx, nk, Q, cplx ? 2 * ldq : ldq, h, r, ctl, skip);
 }
 
 // Classical Gram-Schmidt, applied `passes` times: r -= Q[:nk]^T (conj(Q[:nk]) r).
@@ -263,10 +340,39 @@ extern "C" int qs_lanczos_reorth(int64_t n, int cplx, int nk, const double *Q, i
     int nb = lz_blocks(n);
     double *part = scratch;
     double *h = scratch + (int64_t)2 * LZ_BLOCKS_MAX * nk;
-    for (int p = 0; p < passes; p++) {
-        lz_gemv_t_kernel<<<nb, LZ_THREADS, 0, st>>>(n, cplx, nk, Q, cplx ? 2 * ldq : ldq, r, part, (const LzCtl *)ctl);
-        lz_gemv_t_finish<<<(nk + 127) / 128, 128, 0, st>>>(nb, nk, part, h, (const LzCtl *)ctl);
-        lz_gemv_n_kernel<<<nb, LZ_THREADS, 0, st>>>(n, cplx, nk, Q, cplx ? 2 * ldq : ldq, h, r, (const LzCtl *)ctl);
+    for (int p = 0; p < passes; p++) reorth_pass(st, nb, n, cplx, nk, Q, ldq, r, part, h, (const LzCtl *)ctl, nullptr);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+// The same with the pass count decided on the device (the criterion of
+// Daniel, Gragg, Kaufman and Stewart, Math. Comp. 30 (1976) 772, as ARPACK
+// applies it): after each pass the norm of r is compared with its norm
+// before the pass; if at least 1/sqrt(2) of it remains, r is orthogonal to
+// the rows to working precision and no further pass runs; otherwise another
+// pass follows, up to max_passes.  No host synchronisation.
+extern "C" int qs_lanczos_reorth_adaptive(int64_t n, int cplx, int nk, const double *Q, int64_t ldq, double *r,
+                                          int max_passes, double *scratch, void *ctl, void *stream)
+{
+    if (n < 0 || nk < 0 || max_passes < 1 || !Q || !r || !scratch || !ctl) return QS_ERR_ARG;
+    if (nk == 0) return QS_OK;
+    cudaStream_t st = qs_stream(stream);
+    const int nb = lz_blocks(n);
+    const int64_t n2 = cplx ? 2 * n : n;
+    const int nbn = lz_blocks(n2);
+    double *part = scratch;
+    double *h = scratch + (int64_t)2 * LZ_BLOCKS_MAX * nk;
+    double *state = h + 2 * (int64_t)nk;
+    double *npart = state + 2;
+    const LzCtl *c = (const LzCtl *)ctl;
+    lz_axpy_norm_kernel<<<nbn, LZ_THREADS, 0, st>>>(n2, r, nullptr, nullptr, npart, c, 0);
+    lz_dgks_kernel<<<1, LZ_THREADS, 0, st>>>(nbn, npart, state, 1, c);
+    for (int p = 0; p < max_passes; p++) {
+        reorth_pass(st, nb, n, cplx, nk, Q, ldq, r, part, h, c, p == 0 ? nullptr : state + 1);
+        if (p + 1 < max_passes) {
+            lz_axpy_norm_kernel<<<nbn, LZ_THREADS, 0, st>>>(n2, r, nullptr, nullptr, npart, c, 0);
+            lz_dgks_kernel<<<1, LZ_THREADS, 0, st>>>(nbn, npart, state, 0, c);
+        }
     }
     QS_CHECK(cudaGetLastError());
     return QS_OK;

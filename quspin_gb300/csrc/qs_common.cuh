@@ -22,7 +22,7 @@
 #define QS_PF8 6       // real float-pair values as codes: QS_CODE_TABLE pairs, then one uint8 code per nonzero
 #define QS_CPF8 7      // complex float-pair values as codes: QS_CODE_TABLE complex pairs, then one uint8 code each
 #define QS_PF8P 8      // QS_PF8 with each code byte packed into the low 8 bits of its column word (col << 8 | code;
-                       // data holds only the table); single-vector 32-row Taylor term, n < 2^23
+                       // data holds only the table); single-vector Taylor terms and the SpMV, n < 2^23
 #define QS_CPF8P 9     // the same for QS_CPF8
 #define QS_CODE_TABLE 256
 

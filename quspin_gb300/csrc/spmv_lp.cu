@@ -68,9 +68,11 @@ template <class M> __device__ __forceinline__ void st_out(cflt *y, int64_t e, in
     *p = r;
 }
 
-// CODED: data holds a table of QS_CODE_TABLE values followed by one code byte
-// per nonzero (pdtype QS_PF8 / QS_CPF8), the table staged in shared memory.
-template <class M, class DV, bool XC, class YT, class IT, int NB, int U, bool CODED>
+// VM: 0 one value per nonzero; 1 coded: data holds a table of QS_CODE_TABLE
+// values followed by one code byte per nonzero (pdtype QS_PF8 / QS_CPF8);
+// 2 packed: indices holds col << 8 | code and data the table only (QS_PF8P /
+// QS_CPF8P).  The table is staged in shared memory.
+template <class M, class DV, bool XC, class YT, class IT, int NB, int U, int VM>
 __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const IT *__restrict__ indptr,
                                                       const int32_t *__restrict__ indices,
                                                       const DV *__restrict__ data, const void *__restrict__ xv,
@@ -85,6 +87,7 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
     if (threadIdx.x == 0) s_a[0] = M::from_d(a.x);
     if (threadIdx.x == 1) s_a[1] = M::from_d(a.y);
     if (threadIdx.x == 2) s_k = xnorm ? scale_exp(__longlong_as_double((long long)*xnorm)) : 0;
+    constexpr bool CODED = VM != 0;
     __shared__ DV s_tab[CODED ? QS_CODE_TABLE : 1];
     const uint8_t *codes = nullptr;
     if constexpr (CODED) {
@@ -121,9 +124,15 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
                 for (int u = 0; u < U; u++) {
                     const IT kk = k + (IT)(u * G);
                     const bool in = kk < k1;
-                    col[u] = in ? __ldcs(indices + kk) : 0;
-                    if constexpr (CODED) d[u] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
-                    else d[u] = in ? ldv(data + kk) : vzero<DV>();
+                    if constexpr (VM == 2) {
+                        const uint32_t w = in ? (uint32_t)__ldcs(indices + kk) : 0u;
+                        col[u] = (int32_t)(w >> 8);
+                        d[u] = in ? s_tab[w & 255u] : vzero<DV>();
+                    } else {
+                        col[u] = in ? __ldcs(indices + kk) : 0;
+                        if constexpr (VM == 1) d[u] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
+                        else d[u] = in ? ldv(data + kk) : vzero<DV>();
+                    }
                 }
 #pragma unroll
                 for (int u = 0; u < U; u++) {
@@ -212,14 +221,14 @@ static int grid_rows(int64_t n, int G)
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-template <class M, class DV, bool XC, class YT, class IT, int NB, int U, bool CODED>
+template <class M, class DV, bool XC, class YT, class IT, int NB, int U, int VM>
 int spmv_go(const SpmvArgs &a)
 {
     int lg = 0;
     while ((1 << lg) < a.G) lg++;
     // persistent grid (grid-stride kernel): one wave of resident blocks
     static int resident = 0;
-    auto k = spmv_lp_kernel<M, DV, XC, YT, IT, NB, U, CODED>;
+    auto k = spmv_lp_kernel<M, DV, XC, YT, IT, NB, U, VM>;
     const int blocks = qs_persistent_grid(k, 256, grid_rows(a.n, a.G), resident);
     k<<<blocks, 256, 0, a.st>>>(a.n, lg, (const IT *)a.indptr, a.indices, (const DV *)a.data, a.x, (YT *)a.y,
                                 a.nvec, a.a, a.overwrite, a.xnorm);
@@ -227,31 +236,31 @@ int spmv_go(const SpmvArgs &a)
     return QS_OK;
 }
 
-template <class M, class DV, bool XC, class YT, class IT, bool CODED>
+template <class M, class DV, bool XC, class YT, class IT, int VM>
 int spmv_nb(const SpmvArgs &a)
 {
     if (a.nvec == 1) {
         if constexpr (sizeof(IT) == 4) {
-            if (a.U >= 4) return spmv_go<M, DV, XC, YT, IT, 1, 4, CODED>(a);
-            if (a.U >= 2) return spmv_go<M, DV, XC, YT, IT, 1, 2, CODED>(a);
+            if (a.U >= 4) return spmv_go<M, DV, XC, YT, IT, 1, 4, VM>(a);
+            if (a.U >= 2) return spmv_go<M, DV, XC, YT, IT, 1, 2, VM>(a);
         }
-        return spmv_go<M, DV, XC, YT, IT, 1, 1, CODED>(a);
+        return spmv_go<M, DV, XC, YT, IT, 1, 1, VM>(a);
     }
-    if (a.nvec == 2) return spmv_go<M, DV, XC, YT, IT, 2, 1, CODED>(a);
-    if (a.nvec <= 4) return spmv_go<M, DV, XC, YT, IT, 4, 1, CODED>(a);
-    return spmv_go<M, DV, XC, YT, IT, 8, 1, CODED>(a);
+    if (a.nvec == 2) return spmv_go<M, DV, XC, YT, IT, 2, 1, VM>(a);
+    if (a.nvec <= 4) return spmv_go<M, DV, XC, YT, IT, 4, 1, VM>(a);
+    return spmv_go<M, DV, XC, YT, IT, 8, 1, VM>(a);
 }
 
-// coded values: int32 column indices only
-template <class M, class DV, bool XC, class YT, bool CODED = false>
+// coded and packed values: int32 column indices only
+template <class M, class DV, bool XC, class YT, int VM = 0>
 int spmv_idx(const SpmvArgs &a)
 {
-    if constexpr (CODED) {
+    if constexpr (VM != 0) {
         if (a.idx64) return QS_ERR_ARG;
-        return spmv_nb<M, DV, XC, YT, int32_t, true>(a);
+        return spmv_nb<M, DV, XC, YT, int32_t, VM>(a);
     } else {
-        if (a.idx64) return spmv_nb<M, DV, XC, YT, int64_t, false>(a);
-        return spmv_nb<M, DV, XC, YT, int32_t, false>(a);
+        if (a.idx64) return spmv_nb<M, DV, XC, YT, int64_t, 0>(a);
+        return spmv_nb<M, DV, XC, YT, int32_t, 0>(a);
     }
 }
 
@@ -274,7 +283,9 @@ int spmv_lp_single(int64_t n, const void *indptr, int idx64, const int32_t *indi
 // the matrix values as float pairs (pdtype QS_PF from float64 values,
 // QS_CPF from complex128 values; a complex matrix needs complex x), or as
 // one code byte per nonzero into a table of such pairs (QS_PF8 / QS_CPF8:
-// QS_CODE_TABLE pairs, then nnz uint8 codes; int32 indices).
+// QS_CODE_TABLE pairs, then nnz uint8 codes; int32 indices), or with the
+// code packed into the low 8 bits of each column word (QS_PF8P / QS_CPF8P:
+// indices holds col << 8 | code, col < 2^23; pdata the table only).
 // xs: scratch of n*nvec*(8 or 16) bytes for the split x; norm: 8 bytes of
 // device scratch.  group as for qs_csr_matvec.
 extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
@@ -286,10 +297,12 @@ extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, i
     if (n == 0) return QS_OK;
     const bool xc = xtype == QS_C128;
     if (!xc && xtype != QS_F64) return QS_ERR_ARG;
-    const bool cvals = pdtype == QS_CPF || pdtype == QS_CPF8;
+    const bool cvals = pdtype == QS_CPF || pdtype == QS_CPF8 || pdtype == QS_CPF8P;
     if (!xc && (a_im != 0.0 || cvals)) return QS_ERR_ARG;
-    if (pdtype != QS_PF && pdtype != QS_CPF && pdtype != QS_PF8 && pdtype != QS_CPF8) return QS_ERR_ARG;
-    if ((pdtype == QS_PF8 || pdtype == QS_CPF8) && idx64) return QS_ERR_ARG;
+    if (pdtype != QS_PF && pdtype != QS_CPF && pdtype != QS_PF8 && pdtype != QS_CPF8 && pdtype != QS_PF8P &&
+        pdtype != QS_CPF8P)
+        return QS_ERR_ARG;
+    if (pdtype != QS_PF && pdtype != QS_CPF && idx64) return QS_ERR_ARG;
     int G = group > 0 ? (group & 0xff) : 2;
     int U = group > 0 ? ((group >> 8) & 0xff) : 1;
     if (U < 1) U = 1;
@@ -306,8 +319,10 @@ extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, i
     xsplit_kernel<<<blocks, 256, 0, st>>>(count, (const double *)x, (float2 *)xs, nrm);
     QS_CHECK(cudaGetLastError());
     SpmvArgs s{n, indptr, idx64, indices, pdata, xs, y, nvec, cdbl{a_re, a_im}, overwrite, nrm, G, U, st};
-    if (pdtype == QS_PF8) return xc ? spmv_idx<ModePF, pf, true, cdbl, true>(s) : spmv_idx<ModePF, pf, false, double, true>(s);
-    if (pdtype == QS_CPF8) return spmv_idx<ModePF, cpf, true, cdbl, true>(s);
+    if (pdtype == QS_PF8) return xc ? spmv_idx<ModePF, pf, true, cdbl, 1>(s) : spmv_idx<ModePF, pf, false, double, 1>(s);
+    if (pdtype == QS_CPF8) return spmv_idx<ModePF, cpf, true, cdbl, 1>(s);
+    if (pdtype == QS_PF8P) return xc ? spmv_idx<ModePF, pf, true, cdbl, 2>(s) : spmv_idx<ModePF, pf, false, double, 2>(s);
+    if (pdtype == QS_CPF8P) return spmv_idx<ModePF, cpf, true, cdbl, 2>(s);
     if (!xc) return spmv_idx<ModePF, pf, false, double>(s);
     if (pdtype == QS_PF) return spmv_idx<ModePF, pf, true, cdbl>(s);
     return spmv_idx<ModePF, cpf, true, cdbl>(s);

@@ -133,8 +133,12 @@ class DeviceCSR:
             if P is None:
                 self._nprod = self.__dict__.get("_nprod", 0) + 1
                 P = self.paired(coded=self._nprod > self.CODE_AFTER_PRODUCTS)
+            # a coded operand reads its code bytes from the column words
+            Pk = P.packed() if P.coded else None
+            if Pk is not None:
+                P = Pk
             xs, nrm = self._pair_scratch(x.numel() * (2 if xt.kind == "c" else 1))
-            _lib.call("qs_csr_matvec_pairs", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(self.indices),
+            _lib.call("qs_csr_matvec_pairs", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(P.indices),
                       D.ptr(P.data), P.vcode, D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,
                       int(bool(overwrite)), int(group), D.ptr(xs), D.ptr(nrm), D.stream())
             return y

@@ -10,8 +10,10 @@ reference.  ``full_ortho=True`` keeps the reference's post-hoc
 orthonormalisation + projection (:206-222), with the orthonormalisation by
 classical Gram-Schmidt twice and the projection as one FP64 tensor-instruction
 block product (csrc/dense.cu); ``reorth=True`` is this package's per-step full
-reorthogonalisation (classical Gram-Schmidt twice against every previous
-Lanczos vector), for long runs where the plain recurrence loses orthogonality.
+reorthogonalisation (classical Gram-Schmidt against every previous Lanczos
+vector, repeated once only when the first pass removed more than
+1 - 1/sqrt(2) of the norm, the criterion ARPACK applies), for long runs where
+the plain recurrence loses orthogonality.
 """
 from __future__ import annotations
 
@@ -126,8 +128,8 @@ def _recurrence(op, q0, m, eps, Q=None, reorth=False):
             # r -= a_i q_i first, then project out Q[0..i] twice
             _lib.check(L.qs_lanczos_beta(n2, dv(r), D.ptr(a_d[i:i + 1]), dv(qi), 1, D.ptr(ab[2 * m:]), 0.0, i,
                                          D.ptr(scr), D.ptr(ctl), st), "qs_lanczos_beta")
-            _lib.check(L.qs_lanczos_reorth(n, cplx, i + 1, dv(Q), n, dv(r), 2, D.ptr(rscr), D.ptr(ctl), st),
-                       "qs_lanczos_reorth")
+            _lib.check(L.qs_lanczos_reorth_adaptive(n, cplx, i + 1, dv(Q), n, dv(r), 2, D.ptr(rscr), D.ptr(ctl),
+                                                    st), "qs_lanczos_reorth_adaptive")
             _lib.check(L.qs_lanczos_beta(n2, dv(r), None, dv(qi), 0, D.ptr(b_d[i:i + 1]), float(eps), i,
                                          D.ptr(scr), D.ptr(ctl), st), "qs_lanczos_beta")
         else:

@@ -158,8 +158,9 @@ def test_empty_and_tiny_operators(cuda):
 
 def test_coded_values_bit_identical(cuda):
     """Matrices with at most 256 distinct values keep one code byte per
-    nonzero into a table of float pairs: products and whole evolutions are
-    bit-identical to the one-pair-per-nonzero operand."""
+    nonzero into a table of float pairs (also packed into the column words):
+    products and whole evolutions are bit-identical to the
+    one-pair-per-nonzero operand."""
     import torch
     from quspin_gb300 import hamiltonian, spin_basis_general
     from tests.models import chain_maps, xxz_static
@@ -179,18 +180,27 @@ def test_coded_values_bit_identical(cuda):
         assert P1.coded and not P2.coded and P1.distinct <= 256
         n = A.shape[0]
         x = D.to_device(rng.normal(size=(n, 3)) + 1j * rng.normal(size=(n, 3)))
-        ys = []
-        for P in (P1, P2):
-            y = torch.empty_like(x)
-            xs = torch.empty(2 * x.numel() * 2, dtype=torch.float32, device=x.device)
-            nrm = torch.zeros(1, dtype=torch.int64, device=x.device)
-            for g in (0x202, 0x104):
-                _lib.call("qs_csr_matvec_pairs", n, A.nnz, D.ptr(A.indptr), A.idx64, D.ptr(A.indices), D.ptr(P.data),
-                          P.vcode, D.ptr(x), _lib.C128, D.ptr(y), 3, 0.5, -0.25, 1, g, D.ptr(xs), D.ptr(nrm),
-                          D.stream())
-                ys.append(y.clone())
-        assert torch.equal(ys[0], ys[2]) and torch.equal(ys[1], ys[3])
-        np.testing.assert_allclose(D.to_host(ys[0]), (0.5 - 0.25j) * (A.tocsr() @ D.to_host(x)), rtol=0, atol=1e-12)
+        P3 = P1.packed()
+        assert P3.vcode == (_lib.CPF8P if dt == np.complex128 else _lib.PF8P)
+        xr = D.to_device(rng.normal(size=n))
+        xs = torch.empty(2 * x.numel() * 2, dtype=torch.float32, device=x.device)
+        nrm = torch.zeros(1, dtype=torch.int64, device=x.device)
+        for xv, nv, xt, a_im in ((x, 3, _lib.C128, -0.25), (x[:, 0].contiguous(), 1, _lib.C128, -0.25),
+                                 (xr, 1, _lib.F64, 0.0)):
+            if xt == _lib.F64 and dt == np.complex128:
+                continue
+            ys = []
+            for P in (P1, P2, P3):
+                y = torch.empty_like(xv)
+                for g in (0x202, 0x104, 0x408):
+                    _lib.call("qs_csr_matvec_pairs", n, A.nnz, D.ptr(A.indptr), A.idx64, D.ptr(P.indices),
+                              D.ptr(P.data), P.vcode, D.ptr(xv), xt, D.ptr(y), nv, 0.5, a_im, 1, g, D.ptr(xs),
+                              D.ptr(nrm), D.stream())
+                    ys.append(y.clone())
+            for i in range(3):
+                assert torch.equal(ys[i], ys[3 + i]) and torch.equal(ys[i], ys[6 + i]), (nv, xt, i)
+            np.testing.assert_allclose(D.to_host(ys[0]), (0.5 + 1j * a_im) * (A.tocsr() @ D.to_host(xv)), rtol=0,
+                                       atol=1e-12)
         v = rng.normal(size=n) + 1j * rng.normal(size=n)
         v /= np.linalg.norm(v)
         outs = []
