@@ -85,6 +85,7 @@ def zeros(shape, dtype):
 # staging buffer (page-locked copies run at the link rate; pageable ones are
 # staged by the driver in small pieces).
 _STAGE_MIN_BYTES = 1 << 20
+_STAGE_MAX_BYTES = 256 << 20          # larger transfers go through the page-locked buffer in chunks
 _stage = {}
 
 
@@ -122,10 +123,14 @@ def to_device(a, dtype=None):
     arr = np.ascontiguousarray(arr)
     if arr.nbytes < _STAGE_MIN_BYTES or arr.dtype.kind not in "iufc" or _pinned(arr):
         return torch.from_numpy(arr).to(device())
-    st = _staging(arr.nbytes)
-    st.numpy()[...] = arr.reshape(-1).view(np.uint8)
     out = torch.empty(arr.shape, dtype=torch_dtype(arr.dtype), device=device())
-    out.view(-1).view(torch.uint8).copy_(st)           # synchronous: the staging buffer is free afterwards
+    src, dst = arr.reshape(-1).view(np.uint8), out.view(-1).view(torch.uint8)
+    step = min(arr.nbytes, _STAGE_MAX_BYTES)
+    st = _staging(step)
+    for o in range(0, arr.nbytes, step):
+        k = min(step, arr.nbytes - o)
+        st.numpy()[:k] = src[o:o + k]
+        dst[o:o + k].copy_(st[:k])                     # synchronous: the staging buffer is free afterwards
     return out
 
 
@@ -134,9 +139,14 @@ def to_host(t, dtype=None):
     nbytes = t.numel() * t.element_size()
     if t.is_cuda and nbytes >= _STAGE_MIN_BYTES and t.dtype in _TORCH_TO_NP:
         tc = t.contiguous()
-        st = _staging(nbytes)
-        st.copy_(tc.view(-1).view(torch.uint8))            # page-locked device-to-host copy
-        arr = st.numpy().view(np_dtype(tc.dtype)).reshape(tuple(tc.shape)).copy()
+        arr = np.empty(tuple(tc.shape), dtype=np_dtype(tc.dtype))
+        src, dst = tc.view(-1).view(torch.uint8), arr.reshape(-1).view(np.uint8)
+        step = min(nbytes, _STAGE_MAX_BYTES)
+        st = _staging(step)
+        for o in range(0, nbytes, step):
+            k = min(step, nbytes - o)
+            st[:k].copy_(src[o:o + k])                     # page-locked device-to-host copy
+            dst[o:o + k] = st[:k].numpy()
     else:
         arr = t.cpu().numpy()
     if dtype is not None and arr.dtype != np.dtype(dtype):

@@ -415,7 +415,7 @@ class ExpmMultiplyParallel:
         self.run_device(F, tol=tol)
         if host:
             res = D.to_host(F)
-            res = res.astype(v_dtype) if v_dtype.kind == "c" else res.real.astype(v_dtype)
+            res = res.astype(v_dtype, copy=False) if v_dtype.kind == "c" else res.real.astype(v_dtype)
             if overwrite_v:
                 v[...] = res
                 return v

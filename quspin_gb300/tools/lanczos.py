@@ -191,10 +191,10 @@ def lanczos_full(A, v0, m, full_ortho=False, out=None, eps=None, reorth=False, p
         if D.is_device_array(out):
             out[:m].copy_(Qm.to(out.dtype))
             return E, V, out[:m]
-        out[:m] = D.to_host(Qm).astype(dtype)
+        out[:m] = D.to_host(Qm).astype(dtype, copy=False)
         return E, V, out[:m]
     if host:
-        return E, V, D.to_host(Qm).astype(dtype)
+        return E, V, D.to_host(Qm).astype(dtype, copy=False)
     return E, V, Qm.to(D.torch_dtype(dtype))
 
 
@@ -223,7 +223,7 @@ class _lanczos_vec_iter:
         dummy = D.scratch_doubles(1)
         ctl = torch.zeros(2, dtype=torch.int32, device=D.device())
         dv = lambda t: D.ptr(torch.view_as_real(t) if t.is_complex() else t)
-        out = lambda t: D.to_host(t).astype(self._dtype) if self._host else t.clone()
+        out = lambda t: D.to_host(t).astype(self._dtype, copy=False) if self._host else t.clone()
         self._op(q, r)
         _lib.check(L.qs_lanczos_alpha(n, cplx, dv(r), None, None, dv(q), D.ptr(dummy), D.ptr(scr), D.ptr(ctl), st),
                    "qs_lanczos_alpha")
@@ -299,9 +299,9 @@ def lin_comb_Q_T(coeff, Q_T, out=None):
         if D.is_device_array(out):
             out.copy_(res.to(out.dtype))
         else:
-            out[...] = D.to_host(res).astype(dtype)
+            out[...] = D.to_host(res).astype(dtype, copy=False)
         return out
-    return D.to_host(res).astype(dtype) if host else res.to(D.torch_dtype(dtype))
+    return D.to_host(res).astype(dtype, copy=False) if host else res.to(D.torch_dtype(dtype))
 
 
 def expm_lanczos(E, V, Q_T, a=1.0, out=None):
