@@ -146,7 +146,7 @@ def to_host(t, dtype=None):
         for o in range(0, nbytes, step):
             k = min(step, nbytes - o)
             st[:k].copy_(src[o:o + k])                     # page-locked device-to-host copy
-            dst[o:o + k] = st[:k].numpy()
+            torch.from_numpy(dst[o:o + k]).copy_(st[:k])   # host copy on torch's intra-op threads
     else:
         arr = t.cpu().numpy()
     if dtype is not None and arr.dtype != np.dtype(dtype):
