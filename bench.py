@@ -18,10 +18,17 @@ ExpmMultiplyParallel.dot -- the call QuSpin users make
   cpu_baseline  the oracle's OpenMP Taylor loop on the host cores, timed on a
              bounded sample of Taylor terms of the same evolution
 
-The CSR (about 2.5 GB) is far larger than L2 (129 MB), so every Taylor term
-streams it from HBM; no separate L2 flush is needed.
+The operand (0.64 GB of column words with the value codes packed in) and the
+three 75 MB vectors are larger than L2 (129 MB), so every Taylor term streams
+the operand from HBM; no separate L2 flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Other workloads (--workload; one JSON line each, not the benchmark line):
+sectors (26 Ising momentum blocks), driven (learned (m*, s) on a driven
+chain), hubbard (Fermi-Hubbard Lanczos and quench), lanczos (200 iterations
+at L=32), evolve (hamiltonian.evolve), small (the XXZ L=20 case beside the CPU
+oracle), spmv (hamiltonian.dot's product alone).
 """
 import argparse
 import ctypes
@@ -39,8 +46,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(workload="j1j2_chain_L32_Sz0_k0_p+1_z+1_expm_t5", L=32, J1=1.0, J2=0.5, t=5.0,
                 sector="Sz=0,k=0,p=+1,z=+1", state="seeded normalised complex128 Gaussian (seed 0)",
-                l2="inputs larger than L2 (every Taylor term streams the CSR operand, 0.64 GB of column indices "
-                   "plus 0.16 GB of value codes, and reads and writes the 75 MB term vectors and the 75 MB "
+                l2="inputs larger than L2 (every Taylor term streams the CSR operand, 0.64 GB of column words "
+                   "carrying the value codes, and reads and writes the 75 MB term vectors and the 75 MB "
                    "partial sum; L2 is 129 MB)")
 FALLBACK_HBM_GBS = 6800.0
 
@@ -308,12 +315,14 @@ def time_kernels(op, F, reps=20):
     return t_term, t_spmv, group, t_ieee, group_ieee, t_spmm8
 
 
-def gather_probe(A, F, reps=10):
+def gather_probe(A, F, reps=10, words=None):
     """The gather-rate floor for this matrix (bench_gather_probe in
     bench_probe.cu, built into _build/libqsprobe.so: the product's row
     hand-out and its random 16-byte gathers of the vector, no values, no
     arithmetic, no epilogue), fastest of G = 2, 4, 8 lanes per row at 6 or 8
-    blocks per SM.  Returns (ms, G, blocks per SM) or None."""
+    blocks per SM.  words: the padded packed column words, read four per
+    load (else the int32 indices, one per load).  Returns (ms, G, blocks per
+    SM) or None."""
     import torch
     from quspin_gb300 import _device as D
     path = os.path.join(ROOT, "_build", "libqsprobe.so")
@@ -324,11 +333,12 @@ def gather_probe(A, F, reps=10):
     y = torch.empty_like(F)
     st = torch.cuda.current_stream()
     best = None
+    idx = A.indices if words is None else words
     for G in (2, 4, 8):
         for bps in (6, 8):
             def run():
-                rc = probe(ctypes.c_int64(A.shape[0]), D.ptr(A.indptr), D.ptr(A.indices), D.ptr(F), D.ptr(y),
-                           ctypes.c_int(G), ctypes.c_int(bps), D.stream())
+                rc = probe(ctypes.c_int64(A.shape[0]), D.ptr(A.indptr), D.ptr(idx), D.ptr(F), D.ptr(y),
+                           ctypes.c_int(G), ctypes.c_int(bps), ctypes.c_int(0 if words is None else 1), D.stream())
                 if rc:
                     raise RuntimeError("bench_gather_probe returned {}".format(rc))
             for _ in range(2):
@@ -680,6 +690,9 @@ def run_ours(args, rank, ws):
     Pmv = A.paired()
     vb_mv = (Pmv.packed() or Pmv).value_bytes if Pmv.coded else Pmv.value_bytes
     probe = gather_probe(A, v_dev)
+    Pp = A.paired()
+    Pk = Pp.packed() if Pp.coded else None
+    probe4 = gather_probe(A, v_dev, words=Pk.indices) if Pk is not None and Pk.padded else None
     tb = taylor_term_bytes(n, nnz, vb=vb)
     achieved = tb / t_term / 1e9
     # rescale (norm + load) + s (m* terms + norm + load); copy excluded
@@ -705,8 +718,9 @@ def run_ours(args, rank, ws):
                      "peak_source": peak_kind, "traffic": traffic, "traffic_source": traffic_note, "kernel": taylor_kernel_name(group),
                      "algorithmic_bytes_per_launch": tb, "launch_ms": 1e3 * t_term,
                      "launch_shape": {"lanes_per_row": group & 0xff, "entries_in_flight": (group >> 8) & 0xff,
-                                      "blocks_per_sm_cap": ({0: 4, 1: 6} if (group >> 20) & 7 else
-                                                            {0: None, 1: 6, 2: 8}).get((group >> 18) & 3)},
+                                      "blocks_per_sm_cap": ({0: 4, 1: 6, 2: 5} if (group >> 20) & 7 else
+                                                            {0: None, 1: 6, 2: 8}).get((group >> 18) & 3),
+                                      "column_words_per_load": 4 if (group >> 20) & 7 in (6, 7) else 1},
                      "operand": "codes packed in the column words" if vb == 0 else "coded values",
                      "value_bytes_per_nonzero": vb, "distinct_values": getattr(P, "distinct", None),
                      "gathers_per_s": nnz / t_term,
@@ -714,6 +728,10 @@ def run_ours(args, rank, ws):
                          "ms": probe[0], "lanes_per_row": probe[1], "blocks_per_sm": probe[2],
                          "gathers_per_s": nnz / (probe[0] / 1e3),
                          "kernel_time_over_probe": 1e3 * t_term / probe[0]},
+                     "gather_probe_words4": None if probe4 is None else {
+                         "ms": probe4[0], "lanes_per_row": probe4[1], "blocks_per_sm": probe4[2],
+                         "gathers_per_s": nnz / (probe4[0] / 1e3),
+                         "kernel_time_over_probe": 1e3 * t_term / probe4[0]},
                      "spmv_gbs": spmv_bytes(n, nnz, vb=vb_mv) / t_spmv / 1e9, "spmv_ms": 1e3 * t_spmv,
                      "spmm8_gbs": spmv_bytes(n, nnz, 8, vb=vb_mv) / t_spmm8 / 1e9, "spmm8_ms": 1e3 * t_spmm8,
                      "spmv_value_bytes_per_nonzero": vb_mv,
@@ -1007,6 +1025,66 @@ def run_hubbard(args):
     print(json.dumps(out))
 
 
+def run_spmv(args):
+    """hamiltonian.dot's product alone on the J1-J2 chain (L=32 default:
+    4,707,969 states, 159.3M nonzeros): y = H x for a seeded normalised
+    complex128 state, in the default float-pair form (the coded operand with
+    the codes packed into the column words, built after the first 64
+    products) and in IEEE double; CUDA events around --steps x 20 products
+    after --warmup x 20 (plus the 70 that build the operand).  The matrix
+    (637 MB of packed words) and x (75 MB) together exceed L2, so each
+    product streams the matrix from HBM."""
+    import torch
+    from quspin_gb300.sparse import set_spmv_precision
+    L = args.L
+    t0 = time.perf_counter()
+    b, H = build_problem(L, 1.0, 0.5)
+    A = H.tocsr_gpu()
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    n, nnz = A.shape[0], A.nnz
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    x = torch.tensor(x / np.linalg.norm(x), device="cuda")
+    y = torch.empty_like(x)
+    st = torch.cuda.current_stream()
+    peak, peak_kind = peak_hbm()
+    res = {}
+    for prec in ("double", "ieee"):
+        old = set_spmv_precision(prec)
+        for _ in range(70 + 20 * args.warmup):
+            A.matvec_into(x, y)
+        torch.cuda.synchronize()
+        reps = 20 * args.steps
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            A.matvec_into(x, y)
+        e1.record(st)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / reps
+        set_spmv_precision(old)
+        if prec == "double":
+            P = A.paired()
+            vb = (P.packed() or P).value_bytes if P.coded else P.value_bytes
+            vcode = A._spmv_operand().vcode
+        else:
+            vb, vcode = 8, None
+        code = A.__dict__.get("_tuned", {}).get(("spmv", 1, np.dtype(np.complex128).str, prec, vcode), 0)
+        nb = spmv_bytes(n, nnz, vb=vb)
+        res[prec] = {"ms": 1e3 * t, "algorithmic_bytes": nb, "value_bytes_per_nonzero": vb, "gbs": nb / t / 1e9,
+                     "frac_of_hbm_peak": nb / t / 1e9 / peak, "y_checksum": complex(y.sum().item()),
+                     "launch_shape": {"lanes_per_row": code & 0xff, "entries_in_flight": (code >> 8) & 0xff,
+                                      "column_words_per_load": 4 if (code >> 20) & 7 == 6 else 1}}
+    ref = res["ieee"]["y_checksum"]
+    out = {"workload": "j1j2_chain_L{}_spmv".format(L), "Ns": n, "nnz": nnz, "build_s": t_build,
+           "peak_gbs": peak, "peak_source": peak_kind, "float_pair": res["double"], "ieee": res["ieee"],
+           "checksum_rel_diff": abs(res["double"]["y_checksum"] - ref) / max(abs(ref), 1e-300)}
+    for r in (out["float_pair"], out["ieee"]):
+        r["y_checksum"] = [r["y_checksum"].real, r["y_checksum"].imag]
+    print(json.dumps(out))
+
+
 def run_lanczos(args):
     """Lanczos at GPU scale: the J1-J2 chain L=32 (Sz=0, k=0, p=+1, z=+1,
     4,707,969 states), 200 iterations with full reorthogonalisation from a
@@ -1270,7 +1348,7 @@ def main():
     p.add_argument("--L", type=int, default=32, help="chain length (32 = the benchmark; smaller for profiling)")
     p.add_argument("--periods", type=int, default=10, help="drive periods of the driven workload")
     p.add_argument("--workload", default="j1j2", choices=["j1j2", "sectors", "driven", "hubbard", "lanczos",
-                                                           "evolve", "small"],
+                                                           "evolve", "small", "spmv"],
                    help="j1j2: the benchmark line; sectors: the many-sector Ising workload (L=24 default)")
     args = p.parse_args()
     if args.L != 32 and args.workload == "j1j2":
@@ -1295,6 +1373,9 @@ def main():
         return
     if args.workload == "small":
         run_small(args)
+        return
+    if args.workload == "spmv":
+        run_spmv(args)
         return
     if args.impl == "reference":
         rank, ws = dist_setup("gloo")

@@ -163,8 +163,13 @@ int qs_csr_1_norm(int64_t n, const void *d_indptr, int idx64, const int32_t *d_i
 int qs_expm_ctl_bytes(void);
 /* Taylor-term storage (btype): 3 = complex128 with IEEE double products;
  * 5 = float pairs with FP32-instruction products (values from qs_split_pairs,
- * dtype 4 / 5); 2 = complex64 with float32 / complex64 values.  F, the
- * shift, the coefficients and the stopping test are double in all three. */
+ * dtype 4 / 5, or coded / packed, dtype 6..9); 2 = complex64 with float32 /
+ * complex64 values.  F, the shift, the coefficients and the stopping test
+ * are double in all three.  group (0: defaults) is a launch code: bits 0-7
+ * lanes per row, 8-15 entries in flight, 18-19 a register cap, 20-22 the
+ * single-vector kernel (1..3 32-row, 4..5 row hand-out, 6..7 row hand-out
+ * reading packed column words four per 16-byte load: dtype 8 / 9 only, with
+ * d_indices readable up to the next multiple of four words). */
 int qs_split_pairs(int64_t count, const double *d_src, void *d_dst, void *stream);
 int qs_taylor_term(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                    const void *d_data, int dtype, const void *d_Bin, void *d_Bout, int btype, void *d_F,

@@ -52,7 +52,8 @@ __device__ __forceinline__ float shfl_idx<ModeF32>(float v, int src)
 
 // VMODE: 0 one value per nonzero (data), 1 coded values (table, then one code
 // byte per nonzero), 2 coded values with the code packed into the column word
-// (indices holds col << 8 | code; data holds the table only).
+// (indices holds col << 8 | code; data holds the table only), 3 the packed
+// form read four words per 16-byte load (row hand-out kernel only).
 template <class M, class DV, int VMODE, int G, int U>
 __device__ __forceinline__ void r32_body(int64_t n, const int32_t *__restrict__ indptr,
                                          const int32_t *__restrict__ indices, const DV *__restrict__ data,
@@ -242,26 +243,46 @@ __device__ __forceinline__ void rows_body(int64_t n, const int32_t *__restrict__
             fv = __ldcs(reinterpret_cast<const double *>(F + r) + comp);
         }
         S ar = M::zero(), ai = M::zero();
-        for (int32_t k = k0 + lane; k < k1; k += G * U) {
-            int32_t col[U];
-            DV d[U];
+        if constexpr (VMODE == 3) {
+            // the row's column words in 16-byte aligned groups of four, group
+            // g of the row to lane g mod G; words outside [k0, k1) are skipped
+            for (int32_t c = (k0 & ~3) + 4 * lane; c < k1; c += 4 * G) {
+                const uint4 w4 = __ldcs(reinterpret_cast<const uint4 *>(indices + c));
+                const uint32_t w[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
-            for (int uu = 0; uu < U; uu++) {
-                const int32_t kk = k + uu * G;
-                const bool in = kk < k1;
-                if constexpr (VMODE == 2) {
-                    const uint32_t w = in ? (uint32_t)__ldcs(indices + kk) : 0u;
-                    col[uu] = (int32_t)(w >> 8);
-                    d[uu] = in ? s_tab[w & 255u] : vzero<DV>();
-                } else {
-                    col[uu] = in ? __ldcs(indices + kk) : 0;
-                    if constexpr (VMODE == 1) d[uu] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
-                    else d[uu] = in ? ldv(data + kk) : vzero<DV>();
+                for (int h = 0; h < 4; h += 2) {     // two gathers in flight, as the U = 2 form
+                    BE bv[2];
+#pragma unroll
+                    for (int i = 0; i < 2; i++)
+                        bv[i] = (c + h + i >= k0 && c + h + i < k1) ? M::ldB(Bin + (int32_t)(w[h + i] >> 8), keep)
+                                                                    : BE{M::zero(), M::zero()};
+#pragma unroll
+                    for (int i = 0; i < 2; i++)
+                        if (c + h + i >= k0 && c + h + i < k1) vmul_acc<M>(ar, ai, s_tab[w[h + i] & 255u], bv[i]);
                 }
             }
+        } else {
+            for (int32_t k = k0 + lane; k < k1; k += G * U) {
+                int32_t col[U];
+                DV d[U];
 #pragma unroll
-            for (int uu = 0; uu < U; uu++)
-                if (k + uu * G < k1) vmul_acc<M>(ar, ai, d[uu], M::ldB(Bin + col[uu], keep));
+                for (int uu = 0; uu < U; uu++) {
+                    const int32_t kk = k + uu * G;
+                    const bool in = kk < k1;
+                    if constexpr (VMODE == 2) {
+                        const uint32_t w = in ? (uint32_t)__ldcs(indices + kk) : 0u;
+                        col[uu] = (int32_t)(w >> 8);
+                        d[uu] = in ? s_tab[w & 255u] : vzero<DV>();
+                    } else {
+                        col[uu] = in ? __ldcs(indices + kk) : 0;
+                        if constexpr (VMODE == 1) d[uu] = in ? s_tab[__ldcs(codes + kk)] : vzero<DV>();
+                        else d[uu] = in ? ldv(data + kk) : vzero<DV>();
+                    }
+                }
+#pragma unroll
+                for (int uu = 0; uu < U; uu++)
+                    if (k + uu * G < k1) vmul_acc<M>(ar, ai, d[uu], M::ldB(Bin + col[uu], keep));
+            }
         }
 #pragma unroll
         for (int o = G >> 1; o > 0; o >>= 1) {
@@ -336,6 +357,11 @@ __global__ void __launch_bounds__(256, 6) taylor_rows_kernel_occ6(R32_PARAMS)
 {
     rows_body<M, DV, VMODE, G, U>(R32_ARGS);
 }
+template <class M, class DV, int VMODE, int G, int U>
+__global__ void __launch_bounds__(256, 5) taylor_rows_kernel_occ5(R32_PARAMS)
+{
+    rows_body<M, DV, VMODE, G, U>(R32_ARGS);
+}
 
 template <class K>
 int r32_blocks(K kern, const LpTerm &a, int &per_sm)
@@ -356,9 +382,11 @@ int rows_go(const LpTerm &a)
 {
     constexpr int U = 2;
     using BE = typename M::BE;
-    static int per_sm[2] = {-1, -1};
-    auto k = a.occ == 1 ? taylor_rows_kernel_occ6<M, DV, VMODE, G, U> : taylor_rows_kernel<M, DV, VMODE, G, U>;
-    int &ps = per_sm[a.occ == 1 ? 1 : 0];
+    static int per_sm[3] = {-1, -1, -1};
+    const int oc = a.occ == 1 || a.occ == 2 ? a.occ : 0;
+    auto k = oc == 1 ? taylor_rows_kernel_occ6<M, DV, VMODE, G, U>
+                     : (oc == 2 ? taylor_rows_kernel_occ5<M, DV, VMODE, G, U> : taylor_rows_kernel<M, DV, VMODE, G, U>);
+    int &ps = per_sm[oc];
     if (ps < 0) {
         int b = 0;
         QS_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 256, 0));
@@ -408,6 +436,10 @@ int r32_g(const LpTerm &a)
     case 3: return r32_go<M, DV, VMODE, 8>(a);
     case 4: return rows_go<M, DV, VMODE, 2>(a);
     case 5: return rows_go<M, DV, VMODE, 4>(a);
+    case 6:
+    case 7:
+        if constexpr (VMODE == 2) return a.staged == 6 ? rows_go<M, DV, 3, 2>(a) : rows_go<M, DV, 3, 4>(a);
+        else return QS_ERR_ARG;
     default: return QS_ERR_ARG;
     }
 }
@@ -416,11 +448,14 @@ int r32_g(const LpTerm &a)
 
 // The single-vector terms of this file: a.staged = 1..3 the 32-row kernel
 // with 4, 2 or 8 lanes per row in the gather loop, 4..5 the persistent
-// row-handout kernel with 2 or 4 lanes per row; a.occ = 1: registers capped
-// for 6 blocks per SM, else 4.  One vector, int32 indptr and indices.
+// row-handout kernel with 2 or 4 lanes per row, 6..7 the same with the
+// packed column words read in aligned groups of four (packed operands only;
+// the word buffer must be readable up to the next multiple of four words);
+// a.occ = 1: registers capped for 6 blocks per SM, 2 (row hand-out only): 5,
+// else 4.  One vector, int32 indptr and indices.
 int st_taylor_term(const LpTerm &a)
 {
-    if (a.nvec != 1 || a.idx64 || a.staged < 1 || a.staged > 5) return QS_ERR_ARG;
+    if (a.nvec != 1 || a.idx64 || a.staged < 1 || a.staged > 7) return QS_ERR_ARG;
     if (a.btype == QS_CPF) {
         switch (a.dtype) {
         case QS_PF8: return r32_g<ModePF, pf, 1>(a);

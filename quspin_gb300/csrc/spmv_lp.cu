@@ -71,7 +71,9 @@ template <class M> __device__ __forceinline__ void st_out(cflt *y, int64_t e, in
 // VM: 0 one value per nonzero; 1 coded: data holds a table of QS_CODE_TABLE
 // values followed by one code byte per nonzero (pdtype QS_PF8 / QS_CPF8);
 // 2 packed: indices holds col << 8 | code and data the table only (QS_PF8P /
-// QS_CPF8P).  The table is staged in shared memory.
+// QS_CPF8P); 3 packed, one complex vector, the column words read four per
+// 16-byte load (indices readable up to the next multiple of four words).
+// The table is staged in shared memory.
 template <class M, class DV, bool XC, class YT, class IT, int NB, int U, int VM>
 __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const IT *__restrict__ indptr,
                                                       const int32_t *__restrict__ indices,
@@ -117,6 +119,25 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
             S ar[NB], ai[NB];
 #pragma unroll
             for (int b = 0; b < NB; b++) ar[b] = ai[b] = M::zero();
+            if constexpr (VM == 3) {
+                // one vector: the row's packed column words in 16-byte aligned
+                // groups of four, group g of the row to lane g mod G
+                for (IT c = (k0 & ~(IT)3) + 4 * lane; c < k1; c += (IT)(4 * G)) {
+                    const uint4 w4 = __ldcs(reinterpret_cast<const uint4 *>(indices + c));
+                    const uint32_t w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                    for (int h = 0; h < 4; h += 2) {
+                        BE bv[2];
+#pragma unroll
+                        for (int i = 0; i < 2; i++)
+                            bv[i] = (c + h + i >= k0 && c + h + i < k1) ? M::ldB(xc + (int32_t)(w[h + i] >> 8), keep)
+                                                                        : BE{M::zero(), M::zero()};
+#pragma unroll
+                        for (int i = 0; i < 2; i++)
+                            if (c + h + i >= k0 && c + h + i < k1) vmul_acc<M>(ar[0], ai[0], s_tab[w[h + i] & 255u], bv[i]);
+                    }
+                }
+            } else {
             for (IT k = k0 + lane; k < k1; k += (IT)(G * U)) {
                 int32_t col[U];
                 DV d[U];
@@ -148,6 +169,7 @@ __global__ void __launch_bounds__(256) spmv_lp_kernel(int64_t n, int lgG, const 
                         }
                     }
                 }
+            }
             }
 #pragma unroll
             for (int b = 0; b < NB; b++) {
@@ -239,6 +261,10 @@ int spmv_go(const SpmvArgs &a)
 template <class M, class DV, bool XC, class YT, class IT, int VM>
 int spmv_nb(const SpmvArgs &a)
 {
+    if constexpr (VM == 3) {
+        if (a.nvec != 1 || !XC) return QS_ERR_ARG;
+        return spmv_go<M, DV, XC, YT, IT, 1, 1, 3>(a);
+    } else {
     if (a.nvec == 1) {
         if constexpr (sizeof(IT) == 4) {
             if (a.U >= 4) return spmv_go<M, DV, XC, YT, IT, 1, 4, VM>(a);
@@ -249,6 +275,7 @@ int spmv_nb(const SpmvArgs &a)
     if (a.nvec == 2) return spmv_go<M, DV, XC, YT, IT, 2, 1, VM>(a);
     if (a.nvec <= 4) return spmv_go<M, DV, XC, YT, IT, 4, 1, VM>(a);
     return spmv_go<M, DV, XC, YT, IT, 8, 1, VM>(a);
+    }
 }
 
 // coded and packed values: int32 column indices only
@@ -321,8 +348,13 @@ extern "C" int qs_csr_matvec_pairs(int64_t n, int64_t nnz, const void *indptr, i
     SpmvArgs s{n, indptr, idx64, indices, pdata, xs, y, nvec, cdbl{a_re, a_im}, overwrite, nrm, G, U, st};
     if (pdtype == QS_PF8) return xc ? spmv_idx<ModePF, pf, true, cdbl, 1>(s) : spmv_idx<ModePF, pf, false, double, 1>(s);
     if (pdtype == QS_CPF8) return spmv_idx<ModePF, cpf, true, cdbl, 1>(s);
-    if (pdtype == QS_PF8P) return xc ? spmv_idx<ModePF, pf, true, cdbl, 2>(s) : spmv_idx<ModePF, pf, false, double, 2>(s);
-    if (pdtype == QS_CPF8P) return spmv_idx<ModePF, cpf, true, cdbl, 2>(s);
+    const bool v4 = ((group >> 20) & 7) == 6 && group > 0;
+    if (v4 && !(xc && nvec == 1 && (pdtype == QS_PF8P || pdtype == QS_CPF8P))) return QS_ERR_ARG;
+    if (pdtype == QS_PF8P) {
+        if (v4) return spmv_idx<ModePF, pf, true, cdbl, 3>(s);
+        return xc ? spmv_idx<ModePF, pf, true, cdbl, 2>(s) : spmv_idx<ModePF, pf, false, double, 2>(s);
+    }
+    if (pdtype == QS_CPF8P) return v4 ? spmv_idx<ModePF, cpf, true, cdbl, 3>(s) : spmv_idx<ModePF, cpf, true, cdbl, 2>(s);
     if (!xc) return spmv_idx<ModePF, pf, false, double>(s);
     if (pdtype == QS_PF) return spmv_idx<ModePF, pf, true, cdbl>(s);
     return spmv_idx<ModePF, cpf, true, cdbl>(s);

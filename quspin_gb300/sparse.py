@@ -111,32 +111,37 @@ class DeviceCSR:
             self._xs = sc
         return sc
 
-    def matvec_into(self, x, y, a=1.0, overwrite=True, group=None, precision=None):
+    def _spmv_operand(self):
+        """The float-pair operand of the next product: plain pairs for the
+        first CODE_AFTER_PRODUCTS products of a matrix, then the coded form
+        (one sort of the values, worth it for a reused matrix; at once when
+        a Taylor operand exists), with the codes packed into the column words
+        where that applies."""
+        P = self.__dict__.get("_paired_coded")
+        if P is None:
+            self._nprod = self.__dict__.get("_nprod", 0) + 1
+            P = self.paired(coded=self._nprod > self.CODE_AFTER_PRODUCTS)
+        Pk = P.packed() if P.coded else None
+        return P if Pk is None else Pk
+
+    def matvec_into(self, x, y, a=1.0, overwrite=True, group=None, precision=None, operand=None):
         """y (=|+=) a * A x on device tensors of the result dtype.  group:
-        launch shape code (None: the autotuned one for this matrix);
-        precision: "double" / "ieee" for float64 / complex128 vectors (None:
-        the module default)."""
+        launch shape code (None: the autotuned one for this matrix and
+        operand form); precision: "double" / "ieee" for float64 / complex128
+        vectors (None: the module default); operand: the float-pair operand
+        to use (None: the matrix's current one; the tuner pins it)."""
         n = self.shape[0]
         nvec = 1 if x.dim() == 1 else x.shape[1]
         xt = D.np_dtype(x.dtype)
         prec = SPMV_PRECISION if precision is None else precision
         paired = (prec == "double" and xt in (np.dtype(np.float64), np.dtype(np.complex128))
                   and not (self.dtype.kind == "c" and xt.kind != "c"))
+        P = (operand if operand is not None else self._spmv_operand()) if paired else None
         if group is None:
             from .tune import tune_spmv
-            group = tune_spmv(self, nvec, xt, prec)
+            group = tune_spmv(self, nvec, xt, prec, operand=P)
         a = complex(a)
         if paired:
-            # the coded operand costs one sort of the values; build it for a
-            # matrix that has been reused (or when a Taylor operand exists)
-            P = self.__dict__.get("_paired_coded")
-            if P is None:
-                self._nprod = self.__dict__.get("_nprod", 0) + 1
-                P = self.paired(coded=self._nprod > self.CODE_AFTER_PRODUCTS)
-            # a coded operand reads its code bytes from the column words
-            Pk = P.packed() if P.coded else None
-            if Pk is not None:
-                P = Pk
             xs, nrm = self._pair_scratch(x.numel() * (2 if xt.kind == "c" else 1))
             _lib.call("qs_csr_matvec_pairs", n, self.nnz, D.ptr(self.indptr), self.idx64, D.ptr(P.indices),
                       D.ptr(P.data), P.vcode, D.ptr(x), D.code(xt), D.ptr(y), nvec, a.real, a.imag,
@@ -378,9 +383,11 @@ class PairedCSR:
 class PackedCodedCSR:
     """A coded PairedCSR with each nonzero's code byte packed into the low 8
     bits of its column word (col << 8 | code, type codes PF8P / CPF8P): the
-    single-vector Taylor term (csrc/expm_st.cu) then reads one 4-byte word
-    per nonzero instead of a 4-byte index and a 1-byte code.  ``data`` holds
-    the 256-entry pair table only.  Needs fewer than 2^23 columns and int32
+    single-vector Taylor term (csrc/expm_st.cu) and the SpMV then read one
+    4-byte word per nonzero instead of a 4-byte index and a 1-byte code.
+    ``data`` holds the 256-entry pair table only; ``indices`` is zero-padded
+    to a multiple of four words plus four (``padded``), for the kernels that
+    load the words four at a time.  Needs fewer than 2^23 columns and int32
     indices; built from a coded PairedCSR (``PairedCSR.packed()``)."""
 
     format = "csr"
@@ -395,8 +402,13 @@ class PackedCodedCSR:
         tbytes = PairedCSR.TABLE * (16 if P.complex else 8)
         nnz = P.nnz
         codes = P.data[tbytes:tbytes + nnz].to(torch.int32)
-        self.indices = torch.bitwise_or(torch.bitwise_left_shift(P.indices[:nnz].to(torch.int32), 8), codes)
+        # zero words up to the next multiple of four and four more: the kernels
+        # that read the words in aligned groups of four stay inside the buffer
+        words = torch.zeros((nnz + 3) // 4 * 4 + 4, dtype=torch.int32, device=D.device())
+        torch.bitwise_or(torch.bitwise_left_shift(P.indices[:nnz].to(torch.int32), 8), codes, out=words[:nnz])
         del codes
+        self.indices = words
+        self.padded = True
         self.data = P.data[:tbytes].clone()
         self.coded = True
 

@@ -45,13 +45,17 @@ def r32_candidates(M, nvec, btype):
     """Shapes of the single-vector Taylor terms of csrc/expm_st.cu (bits 20-22
     of the launch code: 1..3 the 32-row kernel with 4, 2 or 8 lanes per row in
     the gather loop, 4..5 the persistent row-handout kernel with 2 or 4 lanes
-    per row; bits 18-19: 0 / 1 for 4 / 6 resident blocks per SM): one vector,
-    float forms, int32 indices."""
+    per row, 6..7 the same with the packed column words read four per load;
+    bits 18-19: 0 / 1 for 4 / 6 resident blocks per SM, 2 for 5 in the
+    row-handout kernel): one vector, float forms, int32 indices."""
     if nvec != 1 or btype == _lib.C128 or getattr(M, "idx64", 0):
         return []
     if M.vcode not in (_lib.PF8, _lib.CPF8, _lib.PF8P, _lib.CPF8P, _lib.PF, _lib.CPF, _lib.F32, _lib.C64):
         return []
-    return [(shape, occ) for shape in (1, 2, 3, 4, 5) for occ in (0, 1)]
+    cands = [(shape, occ) for shape in (1, 2, 3, 4, 5) for occ in (0, 1)]
+    if M.vcode in (_lib.PF8P, _lib.CPF8P) and getattr(M, "padded", False):
+        cands += [(shape, occ) for shape in (6, 7) for occ in (0, 1, 2)]
+    return cands
 
 
 def _time(fn, reps=5):
@@ -67,9 +71,11 @@ def _time(fn, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
-def tune_spmv(M, nvec=1, xdtype=np.complex128, precision="double"):
-    """Fastest launch code for M.matvec_into with nvec columns of xdtype."""
-    key = ("spmv", nvec, np.dtype(xdtype).str, precision)
+def tune_spmv(M, nvec=1, xdtype=np.complex128, precision="double", operand=None):
+    """Fastest launch code for M.matvec_into with nvec columns of xdtype, on
+    the given float-pair operand (plain, coded or packed; timed with that
+    operand pinned, so the products of the tuning do not switch it)."""
+    key = ("spmv", nvec, np.dtype(xdtype).str, precision, getattr(operand, "vcode", None))
     cache = M.__dict__.setdefault("_tuned", {})
     if key in cache:
         return cache[key]
@@ -81,9 +87,12 @@ def tune_spmv(M, nvec=1, xdtype=np.complex128, precision="double"):
     x = torch.ones(shape, dtype=D.torch_dtype(xdtype), device=D.device())
     y = torch.empty_like(x)
     best, best_t = 0, None
-    for G, U in _candidates(n, M.nnz, nvec):
-        code = encode(G, U)
-        t = _time(lambda: M.matvec_into(x, y, group=code, precision=precision))
+    codes = [encode(G, U) for G, U in _candidates(n, M.nnz, nvec)]
+    if (nvec == 1 and np.dtype(xdtype).kind == "c" and getattr(operand, "padded", False)
+            and getattr(operand, "vcode", None) in (_lib.PF8P, _lib.CPF8P)):
+        codes += [encode(G, 1) | (6 << 20) for G in (2, 4)]      # column words read four per load
+    for code in codes:
+        t = _time(lambda: M.matvec_into(x, y, group=code, precision=precision, operand=operand))
         if best_t is None or t < best_t:
             best, best_t = code, t
     cache[key] = best
@@ -117,7 +126,7 @@ def tune_taylor(M, nvec, btype):
     cands += [(G, U, occ << 2) for G, U in occ_candidates(M, nvec, btype) for occ in (1, 2)]
     if getattr(M, "vcode", None) in (_lib.PF8P, _lib.CPF8P):
         cands = []                 # the packed form runs only in the 32-row kernel
-    cands += [({1: 4, 2: 2, 3: 8, 4: 2, 5: 4}[shape], 2, (shape << 4) | (occ << 2))
+    cands += [({1: 4, 2: 2, 3: 8, 4: 2, 5: 4, 6: 2, 7: 4}[shape], 2, (shape << 4) | (occ << 2))
               for shape, occ in r32_candidates(M, nvec, btype)]
     for G, U, ch in cands:
         code = encode(G, U) | (ch << 16)

@@ -210,3 +210,41 @@ def test_coded_values_bit_identical(cuda):
                 op._Ad.__dict__["_paired_coded"] = PairedCSR(op._Ad, coded=False)
             outs.append(op.dot(D.to_device(v)))
         assert torch.equal(outs[0], outs[1])
+
+
+def test_packed_vector_loads_spmv(cuda):
+    """The packed operand read four column words per 16-byte load (launch
+    shape 6, one complex vector): the same products as the one-word form in
+    a different order within each lane; against scipy in float64 at the
+    float-pair rounding of each row's sum of moduli, for 2 and 4 lanes per
+    row, overwrite and accumulate."""
+    import torch
+    import scipy.sparse as sp
+    from quspin_gb300 import _device as D
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import DeviceCSR
+    rng = np.random.default_rng(9)
+    n = 40009
+    A = sp.random(n, n, density=30.0 / n, random_state=3, format="csr")
+    A.data = rng.choice(np.array([0.5, -1.0, 0.25, 2.0]), A.nnz)
+    A = sp.csr_matrix(A + A.T)
+    A.sum_duplicates()
+    Ad = DeviceCSR.from_scipy(A)
+    P = Ad.paired(coded=True)
+    assert P.coded
+    Pk = P.packed()
+    assert Pk.padded
+    xh = rng.normal(size=n) + 1j * rng.normal(size=n)
+    x = D.to_device(xh)
+    xs = torch.empty(4 * n, dtype=torch.float32, device="cuda")
+    nrm = torch.zeros(1, dtype=torch.int64, device="cuda")
+    scale = abs(A) @ abs(xh)
+    for G in (2, 4):
+        for ow in (1, 0):
+            y = D.to_device(np.ones(n, np.complex128) * (0.5 - 0.5j))
+            _lib.call("qs_csr_matvec_pairs", n, A.nnz, D.ptr(Ad.indptr), 0, D.ptr(Pk.indices), D.ptr(Pk.data),
+                      Pk.vcode, D.ptr(x), _lib.C128, D.ptr(y), 1, 0.75, 0.25, ow, G | (1 << 8) | (6 << 20),
+                      D.ptr(xs), D.ptr(nrm), D.stream())
+            ref = (0.75 + 0.25j) * (A @ xh) + (0 if ow else (0.5 - 0.5j))
+            err = np.abs(D.to_host(y) - ref)
+            assert np.all(err <= 1e-13 * (scale + 1.0)), (G, ow)

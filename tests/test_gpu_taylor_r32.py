@@ -121,3 +121,70 @@ def test_r32_evolution_bitwise_equal(cuda):
         out.append(F.cpu().numpy())
     for o in out[1:]:
         assert np.array_equal(out[0].view(np.int64), o.view(np.int64))
+
+
+@pytest.mark.parametrize("complex_vals", [False, True])
+def test_rows_vector_loads_term(cuda, complex_vals):
+    """Row hand-out term reading the packed column words four per 16-byte
+    load (shapes 6 / 7): the same products as the one-word form (shapes
+    4 / 5), summed in a different order within each lane, so the new term, F
+    and the stopping-test norm agree to float-pair rounding; the
+    register-cap variants of one shape are bit-identical."""
+    from quspin_gb300 import _device as D
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tune import encode
+    A = _matrix(n=50003, complex_vals=complex_vals, seed=5)
+    Ad = DeviceCSR.from_scipy(A)
+    n = A.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(2)
+    v = torch.randn(n, dtype=torch.complex128, generator=g).to("cuda")
+    F0 = torch.randn(n, dtype=torch.complex128, generator=g).to("cuda")
+    Bp = torch.empty(n, dtype=torch.complex128, device="cuda")          # float-pair storage
+    _lib.call("qs_split_pairs", 2 * n, D.ptr(v), D.ptr(Bp), D.stream())
+    Pk = Ad.paired(coded=True).packed()
+    assert Pk.padded and Pk.indices.numel() >= (Pk.nnz + 3) // 4 * 4 + 4
+
+    def value(B):          # {re.hi, re.lo, im.hi, im.lo} -> complex128
+        x = B.view(torch.float32).reshape(n, 2, 2).double().sum(-1)
+        return torch.complex(x[:, 0], x[:, 1])
+
+    # reordering a sum moves it by a small multiple of the unit roundoff times
+    # the sum of the moduli of its terms: per-row scale |cf| (|A| |B| + |mu| |B|)
+    vh = v.cpu().numpy()
+    scale = abs(0.03 - 0.02j) * (abs(A) @ abs(vh) + 0.37 * abs(vh))
+    scale_d = torch.tensor(scale, device="cuda")
+    for G, shape_old, shape_new in ((2, 4, 6), (4, 5, 7)):
+        ref = _term(Pk, encode(G, 2) | (shape_old << 20), Bp, F0, _lib.CPF)
+        outs = [_term(Pk, encode(G, 2) | (occ << 18) | (shape_new << 20), Bp, F0, _lib.CPF) for occ in (0, 1, 2)]
+        for o in outs[1:]:
+            assert _same(o[0], outs[0][0]) and _same(o[1], outs[0][1]) and o[2] == outs[0][2]
+        assert bool(((value(outs[0][0]) - value(ref[0])).abs() <= 1e-12 * scale_d).all()), G
+        # F += the new term (in units 2^bexp of the control block: B's scale)
+        assert float((outs[0][1] - ref[1]).abs().max()) <= 1e-12 * float(scale.max()), G
+        assert abs(outs[0][2] - ref[2]) <= 1e-12 * abs(ref[2]), G
+
+
+def test_rows_vector_loads_evolution(cuda):
+    """A whole evolution on the four-words-per-load shape against the
+    one-word shape: the same (m*, s) and states within 1e-13."""
+    from quspin_gb300 import _lib
+    from quspin_gb300.sparse import DeviceCSR
+    from quspin_gb300.tools import ExpmMultiplyParallel
+    from quspin_gb300.tune import encode
+    A = _matrix(seed=6)
+    n = A.shape[0]
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=n) + 1j * rng.normal(size=n)
+    v /= np.linalg.norm(v)
+    out = []
+    for code in (encode(2, 2) | (4 << 20) | (1 << 18), encode(2, 2) | (6 << 20), encode(4, 2) | (7 << 20) | (2 << 18)):
+        op = ExpmMultiplyParallel(DeviceCSR.from_scipy(A), a=-0.8j)
+        M = op.A_device.paired().packed()
+        op._pick = M
+        M.__dict__.setdefault("_tuned", {})[("taylor", 1, _lib.CPF)] = code
+        F = torch.tensor(v, device="cuda")
+        op.run_device(F)
+        out.append(F.cpu().numpy())
+    for o in out[1:]:
+        assert np.linalg.norm(o - out[0]) <= 1e-13 * np.linalg.norm(out[0])
