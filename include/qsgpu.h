@@ -171,6 +171,10 @@ int qs_expm_ctl_bytes(void);
  * reading packed column words four per 16-byte load: dtype 8 / 9 only, with
  * d_indices readable up to the next multiple of four words). */
 int qs_split_pairs(int64_t count, const double *d_src, void *d_dst, void *stream);
+/* The truncated pair of d_src[i] 2^-k (hi: top 24 significant bits, lo: the
+ * rest truncated likewise; zero below the normal float range), the split
+ * the many-vector stopping tests use for their moduli. */
+int qs_split_pairs_trunc(int64_t count, const double *d_src, int k, void *d_dst, void *stream);
 int qs_taylor_term(int64_t n, int64_t nnz, const void *d_indptr, int idx64, const int32_t *d_indices,
                    const void *d_data, int dtype, const void *d_Bin, void *d_Bout, int btype, void *d_F,
                    int64_t nvec, double mu_re, double mu_im, const void *d_coeff, int j, double tol, void *d_ctl,

@@ -74,6 +74,7 @@ _SIGS = {
     "qs_csr_1_norm": (_i, [_i64, _vp, _i, _vp, _vp, _i, _d, _d, _vp, _vp, _vp, _vp]),
     "qs_expm_ctl_bytes": (_i, []),
     "qs_split_pairs": (_i, [_i64, _vp, _vp, _vp]),
+    "qs_split_pairs_trunc": (_i, [_i64, _vp, _i, _vp, _vp]),
     "qs_rk_error_scratch_doubles": (_i, [_i64]),
     "qs_rk_combine": (_i, [_i64, _vp, _vp, _i, _vp, _d, _vp, _vp]),
     "qs_adjoint_axpy": (_i, [_i64, _vp, _vp, _d, _d, _i, _vp]),

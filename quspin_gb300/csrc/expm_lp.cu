@@ -206,8 +206,12 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                     double fv = NB == 1 ? f_pre : __ldcs(fp);
                     fv = M::add_to(fv, mine, bexp);
                     __stcs(fp, fv);
-                    if (NB == 1) md = M::to_d(mine, 0);
-                    fs = fv * s_inv;
+                    if (NB == 1) {
+                        md = M::to_d(mine, 0);
+                        fs = fv * s_inv;
+                    } else {
+                        fs = fv;             // scaled by 2^-bexp in the pair split below
+                    }
                 }
                 if constexpr (NB == 1) {
                     double nb2 = __dmul_rn(md, md), f2 = __dmul_rn(fs, fs);
@@ -217,7 +221,7 @@ __device__ __forceinline__ void taylor_lp_body(int64_t n, int lgG, const IT *__r
                     rfn = f2;
                 } else {
                     const pf bm = writer ? to_pair(mine) : pf{0.f, 0.f};
-                    const pf fm = writer ? pair_of_double(fs) : pf{0.f, 0.f};
+                    const pf fm = writer ? pair_of_double_scaled(fs, bexp) : pf{0.f, 0.f};
                     pf b2 = pf_mul(bm, bm), f2 = pf_mul(fm, fm);
                     b2 = pf_add(b2, shfl_xor_pair(b2, 1));
                     f2 = pf_add(f2, shfl_xor_pair(f2, 1));
@@ -572,6 +576,29 @@ extern "C" int qs_split_pairs(int64_t count, const double *src, void *dst, void 
     if (count == 0) return QS_OK;
     int64_t b = (count + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
     split_pairs_kernel<<<(int)(b > cap ? cap : b), 256, 0, qs_stream(stream)>>>(count, src, (float2 *)dst);
+    QS_CHECK(cudaGetLastError());
+    return QS_OK;
+}
+
+namespace {
+__global__ void split_pairs_trunc_kernel(int64_t count, const double *__restrict__ src, int k, float2 *__restrict__ dst)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const pf v = pair_of_double_scaled(src[i], k);
+        dst[i] = make_float2(v.h, v.l);
+    }
+}
+}  // namespace
+
+// dst[i] = the pair of src[i] 2^-k that the many-vector stopping tests form
+// for their moduli: hi = src[i] 2^-k truncated to 24 significant bits, lo =
+// the rest truncated likewise (zero below the normal float range).
+extern "C" int qs_split_pairs_trunc(int64_t count, const double *src, int k, void *dst, void *stream)
+{
+    if (count < 0 || (count > 0 && (!src || !dst))) return QS_ERR_ARG;
+    if (count == 0) return QS_OK;
+    int64_t b = (count + 255) / 256, cap = (int64_t)qs_num_sms() * 8;
+    split_pairs_trunc_kernel<<<(int)(b > cap ? cap : b), 256, 0, qs_stream(stream)>>>(count, src, k, (float2 *)dst);
     QS_CHECK(cudaGetLastError());
     return QS_OK;
 }

@@ -179,12 +179,26 @@ __device__ __forceinline__ pf shfl_xor_pair(pf a, int o)
     return pf{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
 }
 
-// a double as an unevaluated pair of floats (high part by truncation on the
-// bit pattern, one FP64 subtraction for the rest; O(1) inputs)
-__device__ __forceinline__ pf pair_of_double(double x)
+// x 2^-k (exact, O(1)) as an unevaluated pair of floats, without FP64
+// instructions: the high part is x's top 24 significant bits (d2f_scaled);
+// the rest, x minus that, is exactly the low 29 bits of x's stored
+// significand, made a float here by a leading-zero count and truncated to 24
+// significant bits as d2f_scaled truncates (the same pair as truncating x
+// 2^-k, subtracting the high part in FP64 and truncating the difference).
+// Low parts below the normal float range are zero.
+__device__ __forceinline__ pf pair_of_double_scaled(double x, int k)
 {
-    const float h = d2f_scaled(x, 0);
-    return pf{h, d2f_scaled(x - f2d_scaled(h, 0), 0)};
+    const float h = d2f_scaled(x, k);
+    const uint32_t hi = (uint32_t)__double2hiint(x);
+    const uint32_t m = (uint32_t)__double2loint(x) & 0x1fffffffu;
+    if (m == 0u || (__float_as_uint(h) & 0x7fffffffu) == 0u || (__float_as_uint(h) & 0x7f800000u) == 0x7f800000u)
+        return pf{h, 0.f};
+    const int E = (int)((hi >> 20) & 0x7ffu);
+    const int p = 31 - __clz(m);                     // leading bit of m, 0..28
+    const int ef = E - 948 + p - k;                  // float exponent field of m 2^(E-1075-k)
+    if (ef <= 0) return pf{h, 0.f};
+    const uint32_t frac = (p >= 23 ? (m >> (p - 23)) : (m << (23 - p))) & 0x7fffffu;
+    return pf{h, __uint_as_float((hi & 0x80000000u) | ((uint32_t)ef << 23) | frac)};
 }
 
 __device__ __forceinline__ pf pf_sqrt(pf x)
