@@ -759,8 +759,10 @@ def run_ours(args, rank, ws):
 
 def ising_sector_mats(L, hx=0.9, hz=0.5):
     """All momentum sectors of the mixed-field Ising chain, reflection
-    resolved at k = 0 and k = L/2 (26 blocks at L = 24)."""
+    resolved at k = 0 and k = L/2 (26 blocks at L = 24; even L)."""
     from quspin_gb300 import hamiltonian, spin_basis_general
+    if L % 2:
+        raise ValueError("the sector workload needs an even chain length (k = L/2 is a real sector)")
     s_ = np.arange(L)
     t, p = (s_ + 1) % L, s_[::-1].copy()
     static = [["zz", [[-1.0, i, (i + 1) % L] for i in range(L)]], ["x", [[-hx, i] for i in range(L)]],
