@@ -294,11 +294,13 @@ static int term_idx(int idx64, int64_t n, const void *indptr, const int32_t *ind
 // per lane; C = 1 asks the float forms for the chunk-outer sweep, which takes
 // effect only through qs_taylor_term_rows with a row-sum scratch; bit 17
 // narrows its chunks from 8 to 4 vectors; bits 18-19 cap the registers of the
-// single-vector float-pair shapes for 6 / 8 blocks per SM; bits 20-22 = 1..5
+// single-vector float-pair shapes for 6 / 8 blocks per SM; bits 20-22 = 1..7
 // select a single-vector kernel of csrc/expm_st.cu: 1..3 the 32-row kernel
-// with 4, 2 or 8 lanes per row, 4..5 the persistent row-handout kernel with
-// 2 or 4 lanes per row (bit 18 then caps registers for 6 blocks per SM) --
-// one vector, int32 indices; the packed value forms 8 / 9 run only there);
+// with 4, 2 or 8 lanes per row, 4..7 the persistent row-handout kernel with
+// 2 or 4 lanes per row (bits 18-19 then cap registers for 6 / 5 blocks per
+// SM; 6..7 read packed column words four per load) -- one vector, int32
+// indices; the packed value forms 8 / 9 run only there; with several
+// vectors, 1..3 select the vectors-across-lanes kernel of csrc/expm_vl.cu;
 // 0 picks G from nnz/n and U = 2.
 extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, int idx64, const int32_t *indices,
                                    const void *data, int dtype, const void *Bin, void *Bout, int btype, void *F,
@@ -340,7 +342,7 @@ extern "C" int qs_taylor_term_rows(int64_t n, int64_t nnz, const void *indptr, i
         a.occ = group > 0 ? (group >> 18) & 3 : 0;
         a.nnz = nnz;
         a.staged = group > 0 ? (group >> 20) & 7 : 0;
-        if (a.staged) return st_taylor_term(a);
+        if (a.staged) return a.nvec == 1 ? st_taylor_term(a) : vl_taylor_term(a, false);
         return lp_taylor_term(a, false);
     }
     if (btype == QS_C128) {
@@ -666,6 +668,8 @@ extern "C" int qs_taylor_multi_term_rows(int64_t n, const void *indptr, const in
         LpTerm a{n, indptr, 0, indices, data, dtype, Bin, Bout, btype, Fp, nvec, cdbl{0.0, 0.0}, m, sec_off, cf, j, tol,
                  ctl, G, U, co, co && ((group >> 17) & 1), rownorm, st};
         a.occ = group > 0 ? (group >> 18) & 3 : 0;
+        a.staged = group > 0 ? (group >> 20) & 7 : 0;
+        if (a.staged && nvec > 1) return vl_taylor_term(a, true);
         return lp_taylor_term(a, true);
     }
     if (btype == QS_C128) {

@@ -125,11 +125,14 @@ struct LpTerm {
     cudaStream_t st;
     int occ = 0;              // single-vector float-pair shapes: 1 / 2 cap registers for 6 / 8 blocks per SM
     int64_t nnz = 0;          // stored entries (the staged kernel's copy bounds)
-    int staged = 0;           // 1..5: single-vector kernel of csrc/expm_st.cu (1..3 32-row, 4..5 row hand-out)
+    int staged = 0;           // one vector: kernel of csrc/expm_st.cu (1..3 32-row, 4..7 row hand-out);
+                              // several: 1..3 the vectors-across-lanes kernel of csrc/expm_vl.cu
 };
 
 // The single-vector terms of csrc/expm_st.cu.
 int st_taylor_term(const LpTerm &a);
+// The many-vector terms with the vectors across the lanes (csrc/expm_vl.cu).
+int vl_taylor_term(const LpTerm &a, bool multi);
 
 int lp_taylor_term(const LpTerm &a, bool multi);
 // F = eta F, norms, scale exponent, then B0 = F 2^-bexp in btype storage.

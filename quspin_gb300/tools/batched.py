@@ -133,6 +133,8 @@ class MultiSectorExpm:
                  if not (self.nvec == 1 and U > 2)]
         codes += [encode(G, U) | (occ << 18) for G, U in occ_candidates(self._A, self.nvec, self._btype)
                   for occ in (1, 2)]
+        if self.nvec > 1:      # the vectors-across-lanes kernel (csrc/expm_vl.cu), three shapes
+            codes += [encode(2, 2) | (shape << 20) for shape in (1, 2, 3)]
         for code in codes:
             self._ctl.copy_(self._ctl_tmpl)
             t = _time(lambda: self._term(0, b0, b1, 0.0, code))

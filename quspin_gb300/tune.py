@@ -124,8 +124,11 @@ def tune_taylor(M, nvec, btype):
         cands += [(G, U, 3) for G, U, _ in cands]
         rown = torch.empty(2 * n, dtype=torch.float64, device=D.device())
     cands += [(G, U, occ << 2) for G, U in occ_candidates(M, nvec, btype) for occ in (1, 2)]
+    if nvec > 1 and btype != _lib.C128:
+        # the vectors-across-lanes kernel (csrc/expm_vl.cu), three shapes
+        cands += [(2, 2, shape << 4) for shape in (1, 2, 3)]
     if getattr(M, "vcode", None) in (_lib.PF8P, _lib.CPF8P):
-        cands = []                 # the packed form runs only in the 32-row kernel
+        cands = []                 # the packed form runs only in the single-vector kernels
     cands += [({1: 4, 2: 2, 3: 8, 4: 2, 5: 4, 6: 2, 7: 4}[shape], 2, (shape << 4) | (occ << 2))
               for shape, occ in r32_candidates(M, nvec, btype)]
     for G, U, ch in cands:
