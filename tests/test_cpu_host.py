@@ -120,10 +120,34 @@ def test_consolidate_static_merges_bonds_and_drops_tiny_couplings():
 def test_r32_candidates_need_one_vector_float_forms():
     from quspin_gb300.tune import r32_candidates
 
-    def M(vcode, idx64=0):
-        return type("M", (), {"idx64": idx64, "vcode": vcode})()
+    def M(vcode, idx64=0, padded=False):
+        return type("M", (), {"idx64": idx64, "vcode": vcode, "padded": padded})()
     assert r32_candidates(M(_lib.PF8P), 1, _lib.CPF) == [(s, o) for s in (1, 2, 3, 4, 5) for o in (0, 1)]
+    # the four-words-per-load shapes need the padded packed words
+    assert r32_candidates(M(_lib.PF8P, padded=True), 1, _lib.CPF) == (
+        [(s, o) for s in (1, 2, 3, 4, 5) for o in (0, 1)] + [(s, o) for s in (6, 7) for o in (0, 1, 2)])
+    assert len(r32_candidates(M(_lib.PF8, padded=True), 1, _lib.CPF)) == 10
     assert len(r32_candidates(M(_lib.PF8), 1, _lib.CPF)) == 10
     assert r32_candidates(M(_lib.PF8), 2, _lib.CPF) == []
     assert r32_candidates(M(_lib.PF8), 1, _lib.C128) == []
     assert r32_candidates(M(_lib.PF8, idx64=1), 1, _lib.CPF) == []
+
+
+def test_pair_split_reference_restates_the_definition():
+    """The numpy restatement the bit-exact GPU test of qs_split_pairs_trunc
+    compares with: hi has 24 significant bits, hi + lo has 48, the rest is
+    below 2^-46 of x 2^-k, and both parts are truncations (|hi| <= |x|,
+    |lo| <= |x 2^-k - hi|, same signs)."""
+    from tests.test_gpu_pair_split import _reference
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=50000) * np.exp(rng.uniform(-30, 30, 50000))
+    for k in (0, 7, -5, 30):
+        xs = x * 2.0 ** -k
+        hi, lo = _reference(x, k)
+        h, l_ = hi.astype(np.float64), lo.astype(np.float64)
+        assert np.all(np.abs(xs - h - l_) <= 2.0 ** -46 * np.abs(xs))
+        assert np.all(np.abs(h) <= np.abs(xs)) and np.all(np.abs(l_) <= np.abs(xs - h))
+        assert np.all((h == 0) | (np.sign(h) == np.sign(xs)))
+        assert np.all((l_ == 0) | (np.sign(l_) == np.sign(xs)))
+        # 24 significant bits: the low 29 bits of the float64 pattern are zero
+        assert np.all((h.view(np.uint64) & np.uint64((1 << 29) - 1)) == 0)
