@@ -155,6 +155,23 @@ class DeviceCSR:
     def dot(self, V, out=None, a=1.0, overwrite_out=True):
         return _apply(self, V, out, a, overwrite_out)
 
+    def _conj_transpose_sorted(self):
+        """A^H by one device sort of the (column, row) keys of the stored
+        entries (canonical input: no duplicates to sum, no zeros to drop)."""
+        n, nnz = self.shape[0], self.nnz
+        dev = D.device()
+        counts = (self.indptr[1:] - self.indptr[:-1]).to(torch.int64)
+        rows = torch.repeat_interleave(torch.arange(n, dtype=torch.int64, device=dev), counts)
+        cols = self.indices[:nnz].to(torch.int64)
+        order = torch.argsort(cols * n + rows, stable=True)
+        ccount = torch.bincount(cols, minlength=n)
+        indptr = torch.zeros(n + 1, dtype=self.indptr.dtype, device=dev)
+        indptr[1:] = torch.cumsum(ccount, 0).to(self.indptr.dtype)
+        data = self.data[:nnz][order]
+        if self.dtype.kind == "c":
+            data = data.conj().resolve_conj()
+        return DeviceCSR(indptr, rows[order].to(torch.int32), data.contiguous(), self.shape, self.dtype)
+
     def conj_transpose(self):
         """A^H as a canonical device CSR (built on the device)."""
         n = self.shape[0]
@@ -178,7 +195,9 @@ class DeviceCSR:
         _lib.call("qs_csr_merge", vt, n, D.ptr(cnt), D.ptr(cursor), D.ptr(keys), D.ptr(vals), None, D.ptr(mcount),
                   D.ptr(err), st)
         if int(err.item()) & 8:
-            return DeviceCSR.from_scipy(self.tocsr().conj().T.tocsr(), self.dtype)
+            # a column with more than 512 entries: the merge kernel's per-row
+            # sort does not take it, so sort the (column, row) keys instead
+            return self._conj_transpose_sorted()
         _lib.call("qs_scan_inclusive_i64", D.ptr(mcount), n, D.ptr(scr), st)
         nnz2 = int(mcount[-1].item()) if n else 0
         indptr = torch.empty(n + 1, dtype=self.indptr.dtype, device=D.device())

@@ -154,3 +154,24 @@ def test_conj_transpose(cuda):
     np.testing.assert_array_equal(AH.indptr, ref.indptr)
     np.testing.assert_array_equal(AH.indices, ref.indices)
     np.testing.assert_array_equal(AH.data, ref.data)
+
+
+def test_conj_transpose_long_column(cuda):
+    """A column with more than 512 entries (beyond the merge kernel's per-row
+    sort) is transposed on the device by one sort of the (column, row) keys;
+    the result equals scipy's conjugate transpose."""
+    from quspin_gb300.sparse import DeviceCSR
+    rng = np.random.default_rng(3)
+    n = 5000
+    A = sp.random(n, n, density=4.0 / n, random_state=4, format="lil", dtype=np.complex128)
+    A[:, 17] = (rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1)))       # a full column
+    A = sp.csr_matrix(A)
+    A.sum_duplicates()
+    A.eliminate_zeros()
+    assert A.getcol(17).nnz > 512
+    AH = DeviceCSR.from_scipy(A).conj_transpose().tocsr()
+    ref = sp.csr_matrix(A.conj().T)
+    ref.sort_indices()
+    np.testing.assert_array_equal(AH.indptr, ref.indptr)
+    np.testing.assert_array_equal(AH.indices, ref.indices)
+    np.testing.assert_array_equal(AH.data, ref.data)
