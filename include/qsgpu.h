@@ -290,13 +290,16 @@ int qs_lanczos_lincomb(int64_t n_el, int nk, const double *d_c, int cplx_c, cons
  * full_ortho's re-projection, _lanczos_utils.py:206-222; the reference computes them with
  * numpy dot products).  Q [m, >= n] rows (stride ldq), X [n, >= k] C order (stride ldx) or,
  * with xrows, [k, >= n] rows; W [m, k]; cplx: complex128 interleaved; conj: op = complex
- * conjugate.  FP64 tensor
- * instructions (mma.sync m8n8k4 .f64) for k > 2, FP64 FMA for k <= 2; the contraction
- * is split over n and the partial tiles summed in a fixed order (scratch from
- * qs_block_inner_scratch_doubles). ------------------------------------------------ */
+ * conjugate.  FP64 FMAs on 32 x 32 tiles staged through shared memory (k > 2) or per
+ * output element (k <= 2); the _dmma form uses FP64 tensor instructions (mma.sync m8n8k4
+ * .f64) for k > 2, which on GB300 run on the same FP64 pipe no faster.  The contraction is split over
+ * n and the partial tiles summed in a fixed order (scratch from
+ * qs_block_inner_scratch_doubles, the same for both forms). -------------------------- */
 int64_t qs_block_inner_scratch_doubles(int64_t n, int m, int k, int cplx);
 int qs_block_inner(int64_t n, int m, int k, const double *d_Q, int64_t ldq, const double *d_X, int64_t ldx,
                    int xrows, int cplx, int conj, double *d_W, double *d_scratch, void *stream);
+int qs_block_inner_dmma(int64_t n, int m, int k, const double *d_Q, int64_t ldq, const double *d_X, int64_t ldx,
+                        int xrows, int cplx, int conj, double *d_W, double *d_scratch, void *stream);
 
 #ifdef __cplusplus
 }

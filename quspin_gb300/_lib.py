@@ -115,6 +115,7 @@ _SIGS = {
     "qs_lanczos_lincomb": (_i, [_i64, _i, _vp, _i, _vp, _i64, _i, _vp, _vp]),
     "qs_block_inner_scratch_doubles": (_i64, [_i64, _i, _i, _i]),
     "qs_block_inner": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i64, _i, _i, _i, _vp, _vp, _vp]),
+    "qs_block_inner_dmma": (_i, [_i64, _i, _i, _vp, _i64, _vp, _i64, _i, _i, _i, _vp, _vp, _vp]),
 }
 
 

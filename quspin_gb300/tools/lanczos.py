@@ -8,7 +8,7 @@ GPU with alpha/beta kept in device arrays; only the m x m tridiagonal
 eigenproblem is solved on the host (scipy ``eigh_tridiagonal``), as in the
 reference.  ``full_ortho=True`` keeps the reference's post-hoc
 orthonormalisation + projection (:206-222), with the orthonormalisation by
-classical Gram-Schmidt twice and the projection as one FP64 tensor-instruction
+classical Gram-Schmidt twice and the projection as one tiled FP64
 block product (csrc/dense.cu); ``reorth=True`` is this package's per-step full
 reorthogonalisation (classical Gram-Schmidt against every previous Lanczos
 vector, repeated once only when the first pass removed more than
@@ -341,7 +341,7 @@ def _apply_block(A, X):
 
 
 def _block_inner(Q, X, conj=True, xrows=False):
-    """W = op(Q) X on the device (csrc/dense.cu, FP64 tensor-instruction
+    """W = op(Q) X on the device (csrc/dense.cu, tiled FP64
     panels): Q [m, n] rows, X [n, k] C order or, with xrows, [k, n] rows;
     op = complex conjugate when conj.  Real operands stay real."""
     cplx = Q.is_complex() or X.is_complex()
