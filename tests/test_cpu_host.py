@@ -151,3 +151,29 @@ def test_pair_split_reference_restates_the_definition():
         assert np.all((l_ == 0) | (np.sign(l_) == np.sign(xs)))
         # 24 significant bits: the low 29 bits of the float64 pattern are zero
         assert np.all((h.view(np.uint64) & np.uint64((1 << 29) - 1)) == 0)
+
+
+def test_sorted_conj_transpose_host_logic(monkeypatch):
+    """The sort-based conjugate transpose (used for columns beyond the merge
+    kernel's capacity) is plain torch code: run it on CPU tensors against
+    scipy, with a full column and empty rows."""
+    import scipy.sparse as sp
+    from quspin_gb300 import _device as D
+    from quspin_gb300.sparse import DeviceCSR
+    monkeypatch.setattr(D, "device", lambda: torch.device("cpu"))
+    rng = np.random.default_rng(5)
+    n = 700
+    A = sp.random(n, n, density=0.01, random_state=6, format="lil", dtype=np.complex128)
+    A[:, 3] = rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1))
+    A[10, :] = 0
+    A = sp.csr_matrix(A)
+    A.sum_duplicates()
+    A.eliminate_zeros()
+    M = DeviceCSR(torch.tensor(A.indptr.astype(np.int32)), torch.tensor(A.indices.astype(np.int32)),
+                  torch.tensor(A.data), A.shape, np.complex128)
+    T = M._conj_transpose_sorted()
+    R = sp.csr_matrix(A.conj().T)
+    R.sort_indices()
+    np.testing.assert_array_equal(T.indptr.numpy(), R.indptr)
+    np.testing.assert_array_equal(T.indices.numpy(), R.indices)
+    np.testing.assert_array_equal(T.data.numpy(), R.data)
